@@ -1,0 +1,290 @@
+"""Benchmark: coherent plane-wave compounding frames/s on the GB300.
+
+Workload (default): 11 plane waves (-10..10 deg, 2 deg steps), 128 elements,
+pitch 0.3048 mm, 2048 samples at 20 MHz, 512 x 512 voxels at 0.06 mm,
+2-7 MHz band (622 bins), Hann window, angle_lb(60, 1.5) F-number, RF from
+the seeded point + speckle + cyst model (synthetic: the reference's phantom
+recording is not distributed).  One step = one compounded frame: band DFT of
+the 11 x 128 RF lines and the fused beamformer, inputs resident in HBM.
+
+Prints one JSON line.  ``--impl reference`` times the reference's CPU path
+(das_pw.m, restated in C with OpenMP under oracle/) on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "CPWC frames/s (11 angles, 512x512, 128 el)"
+UNIT = "frames/s"
+L2_FLUSH_BYTES = 512 << 20          # > 129 MB L2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--kernel", default="fused", choices=["fused", "plain"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def workload():
+    from f_number_gb300 import f_numbers, synth, windows
+    wl = synth.cpwc_11_angles(seed=0)
+    return wl, windows.hann(), f_numbers.grating.angle_lb(60.0, 1.5)
+
+
+def config_of(wl, kernel):
+    return {"workload": "cpwc_11angles_128el_2048smp_512x512_2-7MHz_hann_anglelb60",
+            "n_angles": int(wl.angles.size), "n_elements": wl.array.n_elements, "n_samples": wl.n_samples,
+            "grid": [int(wl.positions_x.size), int(wl.positions_z.size)], "band_hz": list(wl.f_bounds),
+            "kernel": kernel, "l2": "flushed between timed steps (512 MB write)", "data": "synthetic seeded RF"}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: das_pw.m restated in C (oracle), bounded sample of voxels
+# ---------------------------------------------------------------------------
+def cpu_das_pw_m(wl, win, fn, seconds, threads=0):
+    from oracle import coracle as CO
+    nx, nz = wl.positions_x.size, wl.positions_z.size
+    rng = np.random.default_rng(123)
+    n_vox = nx * nz
+    th = threads or CO.max_threads()
+
+    def run(n):
+        ix = rng.integers(0, nx, n)
+        iz = rng.integers(0, nz, n)
+        t = time.perf_counter()
+        CO.pw_m(wl.positions_x, wl.positions_z, wl.rf, wl.f_s, wl.angles, wl.array.width, wl.array.pitch, wl.c,
+                wl.f_bounds, 0.0, win.spec(), fn.spec(), "on", ix, iz, threads=th)
+        return time.perf_counter() - t
+
+    n = 2 * th
+    t = run(n)
+    while t < 0.5:
+        n *= 4
+        t = run(n)
+    n = max(th, int(n * seconds / max(t, 1e-3)))
+    t = run(n)
+    fps = n / (t * n_vox)
+    return fps, {"value": fps, "unit": UNIT, "cores": th, "kind": "port",
+                 "sample": "das_pw.m CPU semantics (oracle/fnum_oracle.c) on %d random voxels x 11 angles "
+                           "(%.1f s incl. FFT), scaled to the %d-voxel frame" % (n, t, n_vox)}
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def traffic_from_profiles():
+    p = os.path.join(ROOT, "profiles", "pw_fused_cpwc_512.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p)).get("dram_bytes_per_launch")
+        except (ValueError, OSError):
+            return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    wl, win, fn = workload()
+    vals = []
+    cb = None
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_das_pw_m(wl, win, fn, min(2.0, args.cpu_seconds / 4))
+    per = max(2.0, args.cpu_seconds / max(args.steps, 1))
+    for _ in range(args.steps):
+        fps, cb = cpu_das_pw_m(wl, win, fn, per)
+        vals.append(fps)
+    value = float(np.mean(vals))
+    cb["value"] = value
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": config_of(wl, "cpu"), "cpu_baseline": cb,
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+    from f_number_gb300 import _lib, das
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    wl, win, fn = workload()
+    plan = das.PWPlan(wl.positions_x, wl.positions_z, wl.n_samples, wl.array.n_elements, wl.f_s, wl.angles,
+                      wl.array.width, wl.array.pitch, wl.c, list(wl.f_bounds), 0.0, win, fn, device=local,
+                      compound=True, kernel=args.kernel)
+    rf = torch.tensor(wl.rf, dtype=torch.float32, device=dev)                 # [A, E, T]
+    img = torch.empty((1, plan.n_x, plan.n_z), dtype=torch.complex64, device=dev)
+    wts = torch.empty((plan.n_x, plan.n_z), dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        plan.execute_dft(rf, stream)
+        plan.execute_beamform(img, wts, stream=stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = Clocks(local)
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for s in range(args.steps):
+        flush.zero_()
+        e0, e1, e2 = evs[s]
+        e0.record(stream)
+        plan.execute_dft(rf, stream)
+        e1.record(stream)
+        plan.execute_beamform(img, wts, stream=stream)
+        e2.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(c) for a, b, c in evs]
+    dft_ms = [a.elapsed_time(b) for a, b, c in evs]
+    bf_ms = [b.elapsed_time(c) for a, b, c in evs]
+    total_ms = float(sum(step_ms))
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    info = plan.info()
+    frames = args.steps * world
+    value = frames / (total_ms * 1e-3)
+    ms_per_step = total_ms / args.steps
+
+    # end to end through the public API: pinned host RF (double, MATLAB layout) in, host image out
+    e2e = None
+    if not args.no_e2e:
+        A, E, T = wl.rf.shape
+        pinned = torch.empty((A, E, T), dtype=torch.float64, pin_memory=True)
+        pinned.numpy()[...] = wl.rf
+        host_rf = np.transpose(pinned.numpy(), (2, 1, 0))                     # [T, E, A], Fortran order
+        call = lambda: das.gpu_bf_das_pw_rf(wl.positions_x, wl.positions_z, host_rf, wl.f_s, wl.angles,
+                                           wl.array.width, wl.array.pitch, wl.c, list(wl.f_bounds), 0, win, fn,
+                                           None, local, kernel=args.kernel)
+        for _ in range(2):
+            call()
+        n = max(3, min(args.steps, 10))
+        t0 = time.perf_counter()
+        for _ in range(n):
+            im, _w = call()
+        dt = time.perf_counter() - t0
+        e2e = {"value": n / dt, "unit": UNIT, "h2d_bytes_per_step": int(A * E * T * 8),
+               "d2h_bytes_per_step": int(plan.n_x * plan.n_z * (8 + 4)),
+               "api": "f_number_gb300.gpu_bf_das_pw_rf -> fnum_das_pw (host buffers, pinned RF)"}
+
+    peak = _lib.C.c_double(0.0)
+    _lib.check(_lib.lib().fnum_diag_fp32_peak(local, _lib.C.byref(peak)))
+    bf_avg_ms = float(np.mean(bf_ms))
+    flops = 8.0 * info["active_terms"]
+    achieved = flops / (bf_avg_ms * 1e-3) / 1e12
+    roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+            "frac": achieved / peak.value if peak.value else None, "traffic": traffic_from_profiles(),
+            "kernel": "pw_fused_kernel<1,11>", "work": "8 FLOP per active voxel x element x bin x angle term "
+            "(complex MAC); %d active of %d nominal terms" % (info["active_terms"], info["terms"]),
+            "peak_source": "measured FP32 FMA throughput (fnum_diag_fp32_peak); MEASURED_PEAKS.json "
+            "holds only HBM and bf16 figures"}
+    if rank != 0:
+        return
+    cb = None
+    if not args.no_cpu:
+        _, cb = cpu_das_pw_m(wl, win, fn, args.cpu_seconds)
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32 (double-float phase)", "data": "synthetic",
+           "config": config_of(wl, args.kernel),
+           "gterms_per_s": info["terms"] / (ms_per_step * 1e-3) / 1e9,
+           "stage_ms": {"band_dft": float(np.mean(dft_ms)), "beamform": bf_avg_ms},
+           "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "clocks": clk,
+           "gpu_launches": 2 * args.steps}
+    print(json.dumps(out))
+    plan.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    import __graft_entry__ as g
+    g.build()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1043 @@
+// Host side of the C ABI declared in include/fnum.h: argument validation in
+// the order and with the error identifiers of the reference's MEX gateways,
+// the DFT order / band logic, the F-number classes, device-resident plans and
+// the host-buffer entry points that stand in for the MEX calls.
+#include "../../include/fnum.h"
+#include "fnum_internal.h"
+
+#include <cuda_runtime.h>
+#include <float.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <new>
+#include <vector>
+
+using fnum::dfl;
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// status
+// ---------------------------------------------------------------------------
+struct StatusInfo {
+  int code;
+  const char* id;  // suffix of the MEX identifier
+  const char* text;
+};
+const StatusInfo kStatus[] = {
+    {FNUM_OK, "OK", "success"},
+    {FNUM_ERR_NO_DEVICE, "NoCUDADevices", "Could not find any CUDA-enabled devices!"},
+    {FNUM_ERR_INVALID_DEVICE, "InvalidCUDADevice", "Selected device does not exist!"},
+    {FNUM_ERR_LATERAL_POSITIONS, "InvalidLateralPositions", "Lateral positions must be a real-valued finite vector!"},
+    {FNUM_ERR_AXIAL_POSITIONS, "InvalidAxialPositions", "Axial positions must be a real-valued finite vector!"},
+    {FNUM_ERR_RF_DATA, "InvalidRFData", "RF data must be a real-valued array of valid size!"},
+    {FNUM_ERR_SAMPLING_RATE, "InvalidSamplingRate", "Sampling rate must be positive!"},
+    {FNUM_ERR_STEERING_ANGLE, "InvalidSteeringAngle",
+     "Steering angle must be larger than negative pi over two and smaller than pi over two!"},
+    {FNUM_ERR_ELEMENT_WIDTH, "InvalidElementWidth", "Element width must be positive and finite!"},
+    {FNUM_ERR_ELEMENT_PITCH, "InvalidElementPitch", "Element pitch must be finite and larger than element width!"},
+    {FNUM_ERR_SOUND_SPEED, "InvalidSoundSpeed", "Average speed of sound must be positive and finite!"},
+    {FNUM_ERR_FREQUENCY_BOUND, "InvalidFrequencyBound",
+     "Frequency bounds must be positive, increasing and not exceed the Nyquist frequency!"},
+    {FNUM_ERR_FREQUENCY_BOUNDS, "InvalidFrequencyBounds", "Frequency bounds lead to invalid indices!"},
+    {FNUM_ERR_TIME_SHIFT, "InvalidTimeShift", "Time index must be nonnegative!"},
+    {FNUM_ERR_WINDOW, "InvalidWindow", "Unknown window function or invalid window parameter!"},
+    {FNUM_ERR_F_NUMBER, "InvalidFNumber", "Values of F-number must be nonnegative!"},
+    {FNUM_ERR_NORMALIZATION, "InvalidNormalization", "Unknown normalization!"},
+    {FNUM_ERR_VERBOSITY, "InvalidVerbosityLevel", "Selected verbosity level does not exist!"},
+    {FNUM_ERR_ARGUMENT, "InvalidArgument", "Null pointer or size out of range!"},
+    {FNUM_ERR_CUDA, "CUDAError", "CUDA error!"},
+    {FNUM_ERR_OUT_OF_MEMORY, "CUDAError", "CUDA error: out of device memory!"},
+    {FNUM_ERR_INTERNAL, "InternalError", "Device-side consistency check failed!"},
+    {FNUM_ERR_TX_F_NUMBER, "InvalidTXFNumber", "Values of transmit F-number must be nonnegative!"},
+    {FNUM_ERR_RX_F_NUMBER, "InvalidRXFNumber", "Values of receive F-number must be nonnegative!"},
+};
+
+const StatusInfo* find_status(int s) {
+  for (const auto& e : kStatus)
+    if (e.code == s) return &e;
+  return nullptr;
+}
+
+thread_local char g_id_buf[128];
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return FNUM_OK;
+  if (e == cudaErrorMemoryAllocation) return FNUM_ERR_OUT_OF_MEMORY;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return FNUM_ERR_NO_DEVICE;
+  if (e == cudaErrorInvalidDevice) return FNUM_ERR_INVALID_DEVICE;
+  return FNUM_ERR_CUDA;
+}
+
+#define FNUM_CUDA(call)                      \
+  do {                                       \
+    cudaError_t e_ = (call);                 \
+    if (e_ != cudaSuccess) {                 \
+      (void)cudaGetLastError();              \
+      return cuda_status(e_);                \
+    }                                        \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// F-number classes (+f_numbers/**)
+// ---------------------------------------------------------------------------
+double deg2rad(double d) { return (M_PI / 180.0) * d; }
+
+// +f_numbers/+distance/constant.m:90-120
+void fn_distance_constant(double dist_deg, double F_ub, const double* p, int n, double* v) {
+  const double rad = deg2rad(dist_deg);
+  const double sin_d = sin(rad), opc = 1.0 + cos(rad);
+  const double inv_sin = (sin_d != 0.0) ? 1.0 / sin_d : INFINITY;
+  for (int i = 0; i < n; ++i) {
+    const double pl = p[i];
+    const bool lb = pl >= 1.0 / opc, ub = pl < inv_sin;
+    double val = 0.0;
+    if (!lb && pl >= 0.5) {
+      const double t = 1.0 / pl - 1.0;
+      val = sqrt(1.0 / (t * t) - 1.0) / 2.0;
+    } else if (lb && ub) {
+      const double t = pl * pl;
+      val = (sqrt(2.0 * opc * t - 1.0) + opc * sin_d * t) / (2.0 - 2.0 * sin_d * sin_d * t);
+      val = std::min(val, F_ub);
+    }
+    if (!ub) val = F_ub;
+    v[i] = val;
+  }
+}
+
+// +f_numbers/+grating/angle_lb.m:44-75 with the bounds of grating.m:72-75
+void fn_angle_lb(double a_deg, double F_ub, double dist_deg, const double* p, int n, double* v) {
+  const double thresh = sin(deg2rad(a_deg));
+  const double lower = 1.0 / (1.0 + thresh);
+  const double upper = 1.0 / (1.0 / sqrt(1.0 + (2.0 * F_ub) * (2.0 * F_ub)) + thresh);
+  for (int i = 0; i < n; ++i) {
+    const double pl = p[i];
+    double val = 0.0;
+    if (pl > lower && pl < upper) {
+      const double t = 1.0 / pl - thresh;
+      val = sqrt(1.0 / (t * t) - 1.0) / 2.0;
+    } else if (pl >= upper) {
+      val = F_ub;
+    }
+    v[i] = val;
+  }
+  if (dist_deg >= 0) {
+    std::vector<double> aa(n);
+    fn_distance_constant(dist_deg, INFINITY, p, n, aa.data());
+    for (int i = 0; i < n; ++i) v[i] = std::max(v[i], aa[i]);
+  }
+}
+
+// Brent's minimiser on [a, b] in the Forsythe-Malcolm-Moler "fmin" form
+// (R. P. Brent, Algorithms for Minimization without Derivatives, 1973).
+// Stands in for MATLAB fminbnd with TolX = 1e-4 (directivity.m:116).
+template <typename F>
+double fminbnd(F f, double ax, double bx, double tol) {
+  const double c = 0.5 * (3.0 - sqrt(5.0));
+  const double sqeps = sqrt(DBL_EPSILON);
+  double a = ax, b = bx;
+  double v = a + c * (b - a), w = v, x = v;
+  double e = 0.0, d = 0.0;
+  double fx = f(x), fv = fx, fw = fx;
+  for (int it = 0; it < 500; ++it) {
+    const double xm = 0.5 * (a + b);
+    const double tol1 = sqeps * fabs(x) + tol / 3.0, tol2 = 2.0 * tol1;
+    if (fabs(x - xm) <= tol2 - 0.5 * (b - a)) break;
+    bool golden = true;
+    if (fabs(e) > tol1) {
+      double r = (x - w) * (fx - fv);
+      double q = (x - v) * (fx - fw);
+      double p = (x - v) * q - (x - w) * r;
+      q = 2.0 * (q - r);
+      if (q > 0.0) p = -p;
+      q = fabs(q);
+      r = e;
+      e = d;
+      if (fabs(p) < fabs(0.5 * q * r) && p > q * (a - x) && p < q * (b - x)) {
+        d = p / q;
+        const double u = x + d;
+        if ((u - a) < tol2 || (b - u) < tol2) d = (xm - x) >= 0.0 ? tol1 : -tol1;
+        golden = false;
+      }
+    }
+    if (golden) {
+      e = (x >= xm) ? (a - x) : (b - x);
+      d = c * e;
+    }
+    const double u = (fabs(d) >= tol1) ? x + d : x + (d >= 0.0 ? tol1 : -tol1);
+    const double fu = f(u);
+    if (fu <= fx) {
+      if (u >= x) a = x; else b = x;
+      v = w; fv = fw;
+      w = x; fw = fx;
+      x = u; fx = fu;
+    } else {
+      if (u < x) a = u; else b = u;
+      if (fu <= fw || w == x) {
+        v = w; fv = fw;
+        w = u; fw = fu;
+      } else if (fu <= fv || v == x || v == w) {
+        v = u; fv = fu;
+      }
+    }
+  }
+  return x;
+}
+
+double msinc(double x) {
+  if (x == 0.0) return 1.0;
+  const double y = M_PI * x;
+  return sin(y) / y;
+}
+
+// +f_numbers/+directivity/directivity.m:91-120, obliquity rigid (1) or soft (cos)
+void fn_directivity(double wop, int soft, double att_dB, const double* p, int n, double* v) {
+  const double thresh = pow(10.0, -att_dB / 20.0);
+  for (int i = 0; i < n; ++i) {
+    const double wl = wop * p[i];
+    auto f = [&](double th) {
+      const double ob = soft ? cos(th) : 1.0;
+      return fabs(ob * msinc(wl * sin(th)) - thresh);
+    };
+    const double alpha = fminbnd(f, 0.0, M_PI / 2.0, 1e-4);
+    v[i] = 1.0 / (2.0 * tan(alpha));
+  }
+}
+
+int f_number_values(const fnum_f_number* fn, const double* p, int n, double* v) {
+  fnum_f_number def = {FNUM_F_ANGLE_LB, 0, {70.0, 1.5, 10.0}};  // gpu_bf_das_pw_rf.cu:360-365
+  if (fn == nullptr || fn->kind == FNUM_F_DEFAULT) fn = &def;
+  switch (fn->kind) {
+    case FNUM_F_CONSTANT:
+      if (!(fn->p[0] >= 0)) return FNUM_ERR_F_NUMBER;
+      for (int i = 0; i < n; ++i) v[i] = fn->p[0];
+      return FNUM_OK;
+    case FNUM_F_ANGLE_LB:
+      if (!(fn->p[0] >= 0 && fn->p[0] <= 90 && fn->p[1] >= 0 && fn->p[2] <= 90)) return FNUM_ERR_F_NUMBER;
+      fn_angle_lb(fn->p[0], fn->p[1], fn->p[2], p, n, v);
+      return FNUM_OK;
+    case FNUM_F_DISTANCE_CONSTANT:
+      if (!(fn->p[0] >= 0 && fn->p[0] <= 90 && fn->p[1] > 0)) return FNUM_ERR_F_NUMBER;
+      fn_distance_constant(fn->p[0], fn->p[1], p, n, v);
+      return FNUM_OK;
+    case FNUM_F_DISTANCE_NONE:
+      fn_distance_constant(0.0, INFINITY, p, n, v);
+      return FNUM_OK;
+    case FNUM_F_DIRECTIVITY:
+      if (!(fn->p[0] >= 0 && fn->p[0] <= 1 && fn->p[1] > 0)) return FNUM_ERR_F_NUMBER;
+      fn_directivity(fn->p[0], fn->obliquity == FNUM_OBLIQUITY_SOFT, fn->p[1], p, n, v);
+      return FNUM_OK;
+    case FNUM_F_SZABO:
+      if (!(fn->p[0] >= 0 && fn->p[0] <= 1)) return FNUM_ERR_F_NUMBER;
+      for (int i = 0; i < n; ++i) v[i] = fn->p[0] * p[i] / 1.2;  // szabo.m:86
+      return FNUM_OK;
+    default:
+      return FNUM_ERR_F_NUMBER;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// windows (host reference of +cuda/gpu_bf_windows.cu, double precision)
+// ---------------------------------------------------------------------------
+double window_value(fnum_window w, double l, double L) {
+  if (!(fabs(l) < L)) return 0.0;
+  const double u = fabs(l) / L;
+  switch (w.id) {
+    case FNUM_WINDOW_BOXCAR: return 1.0;
+    case FNUM_WINDOW_HANN: return (1.0 + cos(M_PI * u)) / 2.0;
+    case FNUM_WINDOW_TUKEY: {
+      const double thr = 1.0 - w.parameter;
+      return (u <= thr) ? 1.0 : (1.0 + cos(M_PI * (u - thr) / w.parameter)) / 2.0;
+    }
+    case FNUM_WINDOW_TRIANGULAR: return 1.0 - u;
+    default: return 0.0;
+  }
+}
+
+bool window_ok(fnum_window w) {
+  if (!(w.parameter >= 0.0 && w.parameter <= 1.0)) return false;
+  switch (w.id) {
+    case FNUM_WINDOW_BOXCAR:
+    case FNUM_WINDOW_HANN:
+    case FNUM_WINDOW_TRIANGULAR: return true;
+    case FNUM_WINDOW_TUKEY: return w.parameter > 0.0;
+    default: return false;
+  }
+}
+
+bool finite_vec(const double* v, int n) {
+  for (int i = 0; i < n; ++i)
+    if (!std::isfinite(v[i])) return false;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// band (+cuda/gpu_bf_das_pw_rf.cu:494-556)
+// ---------------------------------------------------------------------------
+struct Band {
+  int N, k_lb, k_ub, K;
+  double coef, add, M;
+};
+
+int compute_band(const double* pz, int nz, int nt, int ne, double fs, double width, double pitch, double c,
+                 const double* fb, double t0, Band* b) {
+  (void)width;
+  const double M = (ne - 1.0) / 2.0;
+  // the MEX pads with the second axial position (gpu_bf_das_pw_rf.cu:525); a
+  // single axial position falls back to the first
+  const double z1 = (nz >= 2) ? pz[1] : pz[0];
+  // element centres in float, as the MEX (gpu_bf_das_pw_rf.cu:498-507)
+  // (the aperture term is a float difference squared in float, gpu_bf_das_pw_rf.cu:525)
+  const float c0 = (float)(pitch * (0 - M)), c1 = (float)(pitch * ((ne - 1) - M));
+  const float apf = c1 - c0;
+  const float ap2 = apf * apf;
+  const int N_pad = (int)ceil((sqrt((double)ap2 + z1 * z1) - z1) * fs / c);
+  const int N = nt + N_pad + 1 - ((nt + N_pad) % 2);
+  const double f_lb = fb ? fb[0] : DBL_MIN, f_ub = fb ? fb[1] : fs / 2.0;
+  const int k_lb = (int)ceil(f_lb * N / fs);
+  const int k_ub = (int)floor(f_ub * N / fs);
+  if (!(k_lb > 0 && k_lb <= k_ub && k_ub < N / 2 + 1)) return FNUM_ERR_FREQUENCY_BOUNDS;
+  b->N = N;
+  b->k_lb = k_lb;
+  b->k_ub = k_ub;
+  b->K = k_ub - k_lb + 1;
+  b->coef = 2.0 * M_PI * fs / (N * c);
+  b->add = 2.0 * M_PI * t0 / N;
+  b->M = M;
+  return FNUM_OK;
+}
+
+// geometry checks shared by both gateways (gpu_bf_das_pw_rf.cu:126-318)
+int check_common(const double* px, int nx, const double* pz, int nz, int nt, int ne, double fs, double width,
+                 double pitch, double c, const double* fb, double t0, int dev) {
+  int n_dev = 0;
+  if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev < 1) {
+    (void)cudaGetLastError();
+    return FNUM_ERR_NO_DEVICE;
+  }
+  if (!px || nx < 1 || !finite_vec(px, nx)) return FNUM_ERR_LATERAL_POSITIONS;
+  if (!pz || nz < 1 || !finite_vec(pz, nz)) return FNUM_ERR_AXIAL_POSITIONS;
+  if (nt < 2 || ne < 2 || ne > 4096) return FNUM_ERR_RF_DATA;
+  if (!(fs > 0) || !std::isfinite(fs)) return FNUM_ERR_SAMPLING_RATE;
+  (void)width;
+  return FNUM_OK;
+}
+
+int check_array(double width, double pitch, double c) {
+  if (!(width > 0 && std::isfinite(width))) return FNUM_ERR_ELEMENT_WIDTH;
+  if (!(pitch > width && std::isfinite(pitch))) return FNUM_ERR_ELEMENT_PITCH;
+  if (!(c > 0 && std::isfinite(c))) return FNUM_ERR_SOUND_SPEED;
+  return FNUM_OK;
+}
+
+int check_band_args(double fs, const double* fb, double t0) {
+  const double f_lb = fb ? fb[0] : DBL_MIN, f_ub = fb ? fb[1] : fs / 2.0;
+  if (!(f_lb > 0)) return FNUM_ERR_FREQUENCY_BOUND;
+  if (!(f_ub > f_lb)) return FNUM_ERR_FREQUENCY_BOUND;
+  if (f_ub > fs / 2) return FNUM_ERR_FREQUENCY_BOUND;
+  if (!(t0 >= 0 && std::isfinite(t0))) return FNUM_ERR_TIME_SHIFT;
+  return FNUM_OK;
+}
+
+int check_device(int dev) {
+  int n_dev = 0;
+  if (cudaGetDeviceCount(&n_dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return FNUM_ERR_NO_DEVICE;
+  }
+  // the MEX test (index >= 0 || index < N) is always true (gpu_bf_das_pw_rf.cu:460); this is the intended one
+  if (!(dev >= 0 && dev < n_dev)) return FNUM_ERR_INVALID_DEVICE;
+  return FNUM_OK;
+}
+
+dfl to_df(double v) {
+  const float hi = (float)v;
+  const float lo = (float)(v - (double)hi);
+  return make_float2(hi, lo);
+}
+
+// F table of the band; err = status to return for invalid values
+int band_f_table(const fnum_f_number* fn, const double* values, int n_values, const Band& b, double pitch,
+                 double fs, double c, int err, std::vector<double>& F) {
+  F.assign(b.K, 0.0);
+  if (values) {
+    if (n_values == 1) {
+      for (int i = 0; i < b.K; ++i) F[i] = values[0];
+    } else if (n_values == b.K) {
+      for (int i = 0; i < b.K; ++i) F[i] = values[i];
+    } else {
+      return err;
+    }
+  } else {
+    std::vector<double> pl(b.K);
+    for (int i = 0; i < b.K; ++i) pl[i] = pitch * (b.k_lb + i) * fs / ((double)b.N * c);  // gpu_bf_das_pw_rf.cu:571
+    const int s = f_number_values(fn, pl.data(), b.K, F.data());
+    if (s != FNUM_OK) return err;
+  }
+  for (int i = 0; i < b.K; ++i)
+    if (!(F[i] >= 0 && F[i] <= DBL_MAX)) return err;  // gpu_bf_das_pw_rf.cu:578-587
+  return FNUM_OK;
+}
+
+bool f_monotone(const std::vector<double>& F) {
+  for (size_t i = 1; i < F.size(); ++i) {
+    const double a = ((float)F[i - 1] > FLT_EPSILON) ? F[i - 1] : 0.0;
+    const double b = ((float)F[i] > FLT_EPSILON) ? F[i] : 0.0;
+    if (b < a) return false;
+  }
+  return true;
+}
+
+void g_table(const std::vector<double>& F, std::vector<dfl>& g) {
+  g.resize(F.size());
+  for (size_t i = 0; i < F.size(); ++i)
+    g[i] = ((float)F[i] > FLT_EPSILON) ? to_df(1.0 / (2.0 * F[i])) : make_float2(-1.0f, 0.0f);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// plans
+// ---------------------------------------------------------------------------
+struct fnum_plan {
+  int kind = 0;  // 0 = PW, 1 = SA
+  int flags = 0;
+  int device = 0;
+  int n_out = 1;
+  int grid = 0;
+  Band band{};
+  fnum::PWDev pw{};
+  fnum::SADev sa{};
+  std::vector<void*> allocs;
+  float2* tw = nullptr;
+  float2* X = nullptr;
+  unsigned long long* counters = nullptr;
+  std::vector<double> F, F2;
+  fnum_plan_info info{};
+  int nt = 0;
+
+  template <typename T>
+  int alloc(T** p, size_t count) {
+    void* q = nullptr;
+    const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      return cuda_status(e);
+    }
+    allocs.push_back(q);
+    *p = (T*)q;
+    return FNUM_OK;
+  }
+  template <typename T>
+  int upload(T** p, const std::vector<T>& v) {
+    int s = alloc(p, v.size());
+    if (s) return s;
+    FNUM_CUDA(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return FNUM_OK;
+  }
+  ~fnum_plan() {
+    for (void* p : allocs) cudaFree(p);
+  }
+};
+
+namespace {
+
+// shared geometry tables of both plan kinds
+struct GeomTables {
+  std::vector<dfl> col_u, col_p, col_m, row_u2, row_p, el_u, el_m, el_lb, el_ub;
+  std::vector<int> col_emid;
+  std::vector<float> px_f, pz_f, ctr_f, lb_f, ub_f;
+};
+
+void build_geometry(const double* px, int nx, const double* pz, int nz, int ne, double width, double pitch,
+                    double Ku, double M, GeomTables& g) {
+  std::vector<double> ctr(ne);
+  for (int e = 0; e < ne; ++e) ctr[e] = pitch * (e - M);
+  g.col_u.resize(nx); g.col_p.resize(nx); g.col_m.resize(nx); g.col_emid.resize(nx);
+  for (int i = 0; i < nx; ++i) {
+    g.col_u[i] = to_df(Ku * px[i]);
+    g.col_p[i] = to_df(M + px[i] / pitch);
+    g.col_m[i] = to_df(px[i]);
+    int em = ne;
+    for (int e = 0; e < ne; ++e)
+      if (ctr[e] >= px[i]) { em = e; break; }
+    g.col_emid[i] = em;
+  }
+  g.row_u2.resize(nz); g.row_p.resize(nz);
+  for (int j = 0; j < nz; ++j) {
+    const double zu = Ku * pz[j];
+    // (K_u z)^2 to double-float accuracy
+    const double hi = zu * zu;
+    const double lo = fma(zu, zu, -hi);
+    const float h = (float)hi;
+    g.row_u2[j] = make_float2(h, (float)((hi - (double)h) + lo));
+    g.row_p[j] = to_df(pz[j] / pitch);
+  }
+  g.el_u.resize(ne); g.el_m.resize(ne); g.el_lb.resize(ne); g.el_ub.resize(ne);
+  for (int e = 0; e < ne; ++e) {
+    g.el_u[e] = to_df(Ku * ctr[e]);
+    g.el_m[e] = to_df(ctr[e]);
+    g.el_lb[e] = to_df(ctr[e] - width / 2.0);
+    g.el_ub[e] = to_df(ctr[e] + width / 2.0);
+  }
+  // reference float geometry (gpu_bf_das_pw_rf.cu:495-507, 740-770)
+  g.px_f.resize(nx); g.pz_f.resize(nz); g.ctr_f.resize(ne); g.lb_f.resize(ne); g.ub_f.resize(ne);
+  for (int i = 0; i < nx; ++i) g.px_f[i] = (float)px[i];
+  for (int j = 0; j < nz; ++j) g.pz_f[j] = (float)pz[j];
+  for (int e = 0; e < ne; ++e) {
+    g.ctr_f[e] = (float)(pitch * (e - M));
+    g.lb_f[e] = (float)(g.ctr_f[e] - width / 2);
+    g.ub_f[e] = (float)(g.ctr_f[e] + width / 2);
+  }
+}
+
+template <typename D>
+int upload_geometry(fnum_plan* P, const GeomTables& g, D& d) {
+  int s;
+  dfl* p;
+  int* ip;
+  float* fp;
+  if ((s = P->upload(&p, g.col_u))) return s; d.col_u = p;
+  if ((s = P->upload(&p, g.col_p))) return s; d.col_p = p;
+  if ((s = P->upload(&p, g.col_m))) return s; d.col_m = p;
+  if ((s = P->upload(&ip, g.col_emid))) return s; d.col_emid = ip;
+  if ((s = P->upload(&p, g.row_u2))) return s; d.row_u2 = p;
+  if ((s = P->upload(&p, g.row_p))) return s; d.row_p = p;
+  if ((s = P->upload(&p, g.el_u))) return s; d.el_u = p;
+  if ((s = P->upload(&p, g.el_m))) return s; d.el_m = p;
+  if ((s = P->upload(&p, g.el_lb))) return s; d.el_lb = p;
+  if ((s = P->upload(&p, g.el_ub))) return s; d.el_ub = p;
+  if ((s = P->upload(&fp, g.px_f))) return s; d.px_f = fp;
+  if ((s = P->upload(&fp, g.pz_f))) return s; d.pz_f = fp;
+  if ((s = P->upload(&fp, g.ctr_f))) return s; d.ctr_f = fp;
+  if ((s = P->upload(&fp, g.lb_f))) return s; d.lb_f = fp;
+  if ((s = P->upload(&fp, g.ub_f))) return s; d.ub_f = fp;
+  return FNUM_OK;
+}
+
+int check_pw(const fnum_pw_desc* d, const double* angles, int na) {
+  if (!d) return FNUM_ERR_ARGUMENT;
+  int s = check_common(d->positions_x, d->n_x, d->positions_z, d->n_z, d->n_samples, d->n_elements, d->f_s,
+                       d->element_width, d->element_pitch, d->c_0, d->f_bounds, d->index_t0, d->device);
+  if (s) return s;
+  if (!angles || na < 1) return FNUM_ERR_STEERING_ANGLE;
+  for (int a = 0; a < na; ++a)
+    if (!(angles[a] > -M_PI / 2 && angles[a] < M_PI / 2)) return FNUM_ERR_STEERING_ANGLE;
+  if ((s = check_array(d->element_width, d->element_pitch, d->c_0))) return s;
+  if ((s = check_band_args(d->f_s, d->f_bounds, d->index_t0))) return s;
+  if (!window_ok(d->window)) return FNUM_ERR_WINDOW;
+  if (d->normalization < 0 || d->normalization > 2) return FNUM_ERR_NORMALIZATION;
+  return check_device(d->device);
+}
+
+int check_sa(const fnum_sa_desc* d) {
+  if (!d) return FNUM_ERR_ARGUMENT;
+  int s = check_common(d->positions_x, d->n_x, d->positions_z, d->n_z, d->n_samples, d->n_elements, d->f_s,
+                       d->element_width, d->element_pitch, d->c_0, d->f_bounds, d->index_t0, d->device);
+  if (s) return s;
+  if ((s = check_array(d->element_width, d->element_pitch, d->c_0))) return s;
+  if ((s = check_band_args(d->f_s, d->f_bounds, d->index_t0))) return s;
+  if (!window_ok(d->window_tx) || !window_ok(d->window_rx)) return FNUM_ERR_WINDOW;
+  if (d->normalization_tx < 0 || d->normalization_tx > 2 || d->normalization_rx < 0 || d->normalization_rx > 2)
+    return FNUM_ERR_NORMALIZATION;
+  return check_device(d->device);
+}
+
+int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags, fnum_plan** out) {
+  int s = check_pw(d, angles, na);
+  if (s) return s;
+  FNUM_CUDA(cudaSetDevice(d->device));
+  Band b;
+  if ((s = compute_band(d->positions_z, d->n_z, d->n_samples, d->n_elements, d->f_s, d->element_width,
+                        d->element_pitch, d->c_0, d->f_bounds, d->index_t0, &b)))
+    return s;
+  fnum_plan* P = new (std::nothrow) fnum_plan();
+  if (!P) return FNUM_ERR_OUT_OF_MEMORY;
+  P->kind = 0;
+  P->flags = flags;
+  P->device = d->device;
+  P->band = b;
+  P->nt = d->n_samples;
+  if ((s = band_f_table(&d->f_number, d->f_number_values, d->n_f_number_values, b, d->element_pitch, d->f_s, d->c_0,
+                        FNUM_ERR_F_NUMBER, P->F))) {
+    delete P;
+    return s;
+  }
+  const int nx = d->n_x, nz = d->n_z, ne = d->n_elements;
+  const double Ku = d->f_s / ((double)b.N * d->c_0);
+  GeomTables g;
+  build_geometry(d->positions_x, nx, d->positions_z, nz, ne, d->element_width, d->element_pitch, Ku, b.M, g);
+  fnum::PWDev& D = P->pw;
+  D.nx = nx; D.nz = nz; D.ne = ne; D.na = na; D.K = b.K; D.k_lb = b.k_lb; D.k_ub = b.k_ub; D.N_dft = b.N;
+  D.window_id = d->window.id; D.window_par = (float)d->window.parameter;
+  D.norm = d->normalization != FNUM_NORMALIZATION_OFF;
+  const bool mono = f_monotone(P->F);
+  D.seg_cap = mono ? std::min(b.K, 2 * ne + 16) : b.K;
+  D.flush_chunks = 4;
+  D.scale = (float)(2.0 / b.N);
+  D.x_na = na;
+  D.x_a0 = 0;
+  std::vector<dfl> ax((size_t)na * nx), az((size_t)na * nz), gg;
+  std::vector<float4> txf(na);
+  for (int a = 0; a < na; ++a) {
+    const double ex = -sin(angles[a]), ez = cos(angles[a]);
+    const double xref = (ex >= 0) ? -b.M * d->element_pitch : b.M * d->element_pitch;  // gpu_bf_das_pw_rf.cu:519
+    for (int i = 0; i < nx; ++i) ax[(size_t)a * nx + i] = to_df(Ku * ex * (d->positions_x[i] - xref) + d->index_t0 / b.N);
+    for (int j = 0; j < nz; ++j) az[(size_t)a * nz + j] = to_df(Ku * ez * d->positions_z[j]);
+    txf[a] = make_float4((float)ex, (float)ez, (float)xref, 0.0f);
+  }
+  g_table(P->F, gg);
+  std::vector<float> Ff(b.K);
+  for (int i = 0; i < b.K; ++i) Ff[i] = (float)P->F[i];
+  dfl* p;
+  float* fp;
+  float4* f4;
+  if ((s = upload_geometry(P, g, D)) || (s = P->upload(&p, ax))) goto fail;
+  D.tx_ax = p;
+  if ((s = P->upload(&p, az))) goto fail;
+  D.tx_az = p;
+  if ((s = P->upload(&p, gg))) goto fail;
+  D.g = p;
+  if ((s = P->upload(&fp, Ff))) goto fail;
+  D.F_f = fp;
+  if ((s = P->upload(&f4, txf))) goto fail;
+  D.tx_f = f4;
+  D.M_f = (float)b.M;
+  D.pitch_f = (float)d->element_pitch;
+  D.coef_f = (float)b.coef;
+  D.add_f = (float)b.add;
+  if ((s = P->alloc(&P->tw, b.N))) goto fail;
+  if ((s = P->alloc(&P->X, (size_t)ne * b.K * na))) goto fail;
+  D.X = P->X;
+  if ((s = P->alloc(&P->counters, 4))) goto fail;
+  D.counters = P->counters;
+  {
+    int bps = 0;
+    P->grid = fnum::pw_fused_grid(D, &bps);
+    int4* seg;
+    if ((s = P->alloc(&seg, (size_t)P->grid * fnum::NTHREADS * D.seg_cap))) goto fail;
+    D.seg = seg;
+    P->info.scratch_bytes = (long long)P->grid * fnum::NTHREADS * D.seg_cap * (long long)sizeof(int4);
+  }
+  {
+    cudaError_t e = fnum::launch_twiddles(P->tw, b.N, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+      s = cuda_status(e);
+      goto fail;
+    }
+  }
+  P->n_out = (flags & FNUM_FLAG_COMPOUND) ? 1 : na;
+  P->info.N_dft = b.N; P->info.k_lb = b.k_lb; P->info.k_ub = b.k_ub; P->info.n_bins = b.K;
+  P->info.n_x = nx; P->info.n_z = nz; P->info.n_elements = ne; P->info.n_angles = na; P->info.n_samples = d->n_samples;
+  P->info.f_monotone = mono;
+  P->info.terms = (long long)nx * nz * ne * b.K * na;
+  P->info.scale = 2.0 / b.N;
+  *out = P;
+  return FNUM_OK;
+fail:
+  delete P;
+  return s;
+}
+
+int make_sa_plan(const fnum_sa_desc* d, int flags, fnum_plan** out) {
+  int s = check_sa(d);
+  if (s) return s;
+  FNUM_CUDA(cudaSetDevice(d->device));
+  Band b;
+  if ((s = compute_band(d->positions_z, d->n_z, d->n_samples, d->n_elements, d->f_s, d->element_width,
+                        d->element_pitch, d->c_0, d->f_bounds, d->index_t0, &b)))
+    return s;
+  fnum_plan* P = new (std::nothrow) fnum_plan();
+  if (!P) return FNUM_ERR_OUT_OF_MEMORY;
+  P->kind = 1;
+  P->flags = flags;
+  P->device = d->device;
+  P->nt = d->n_samples;
+  if ((s = band_f_table(&d->f_number_tx, d->f_number_tx_values, d->n_f_number_values, b, d->element_pitch, d->f_s,
+                        d->c_0, FNUM_ERR_TX_F_NUMBER, P->F)) ||
+      (s = band_f_table(&d->f_number_rx, d->f_number_rx_values, d->n_f_number_values, b, d->element_pitch, d->f_s,
+                        d->c_0, FNUM_ERR_RX_F_NUMBER, P->F2))) {
+    delete P;
+    return s;
+  }
+  const bool on_tx = d->normalization_tx != FNUM_NORMALIZATION_OFF;
+  const bool on_rx = d->normalization_rx != FNUM_NORMALIZATION_OFF;
+  const bool intended = (flags & FNUM_FLAG_SAFT_INTENDED) != 0;
+  int last_bin_only = 0;
+  if (!intended && !on_tx && !on_rx) last_bin_only = 1;  // shared buffer cleared every bin (gpu_bf_saft_rf.cu:1128-1148)
+  if (!intended && !on_tx && on_rx) last_bin_only = -1;  // never accumulated (gpu_bf_saft_rf.cu:1195-1199)
+  // restrict the processed band to the single surviving bin
+  Band bk = b;
+  std::vector<double> Ftx = P->F, Frx = P->F2;
+  if (last_bin_only == 1) {
+    bk.k_lb = b.k_ub;
+    bk.K = 1;
+    Ftx.assign(1, P->F.back());
+    Frx.assign(1, P->F2.back());
+  }
+  P->band = bk;
+  const int nx = d->n_x, nz = d->n_z, ne = d->n_elements;
+  const double Ku = d->f_s / ((double)b.N * d->c_0);
+  GeomTables g;
+  build_geometry(d->positions_x, nx, d->positions_z, nz, ne, d->element_width, d->element_pitch, Ku, b.M, g);
+  fnum::SADev& D = P->sa;
+  D.nx = nx; D.nz = nz; D.ne = ne; D.K = bk.K; D.k_lb = bk.k_lb; D.k_ub = bk.k_ub; D.N_dft = b.N;
+  D.wtx_id = d->window_tx.id; D.wtx_par = (float)d->window_tx.parameter;
+  D.wrx_id = d->window_rx.id; D.wrx_par = (float)d->window_rx.parameter;
+  D.norm_tx = on_tx;
+  D.norm_rx = on_rx;
+  D.last_bin_only = last_bin_only;
+  const bool mono = f_monotone(Ftx) && f_monotone(Frx);
+  D.seg_cap = mono ? std::min(bk.K, 4 * ne + 32) : bk.K;
+  D.flush_chunks = 4;
+  D.scale = (float)(2.0 / b.N);
+  std::vector<dfl> gt, gr;
+  g_table(Ftx, gt);
+  g_table(Frx, gr);
+  std::vector<float> Ftf(bk.K), Frf(bk.K);
+  for (int i = 0; i < bk.K; ++i) {
+    Ftf[i] = (float)Ftx[i];
+    Frf[i] = (float)Frx[i];
+  }
+  dfl* p;
+  float* fp;
+  if ((s = upload_geometry(P, g, D)) || (s = P->upload(&p, gt))) goto fail;
+  D.gtx = p;
+  if ((s = P->upload(&p, gr))) goto fail;
+  D.grx = p;
+  if ((s = P->upload(&fp, Ftf))) goto fail;
+  D.Ftx_f = fp;
+  if ((s = P->upload(&fp, Frf))) goto fail;
+  D.Frx_f = fp;
+  D.M_f = (float)b.M;
+  D.pitch_f = (float)d->element_pitch;
+  D.coef_f = (float)b.coef;
+  D.add_f = (float)b.add;
+  if ((s = P->alloc(&P->tw, b.N))) goto fail;
+  if ((s = P->alloc(&P->X, (size_t)ne * ne * bk.K))) goto fail;
+  D.X = P->X;
+  if ((s = P->alloc(&P->counters, 4))) goto fail;
+  D.counters = P->counters;
+  {
+    int bps = 0;
+    P->grid = fnum::sa_fused_grid(D, &bps);
+    int4* seg;
+    if ((s = P->alloc(&seg, (size_t)P->grid * fnum::NTHREADS * D.seg_cap * 2))) goto fail;
+    D.seg = seg;
+    P->info.scratch_bytes = (long long)P->grid * fnum::NTHREADS * D.seg_cap * 2 * (long long)sizeof(int4);
+  }
+  {
+    cudaError_t e = fnum::launch_twiddles(P->tw, b.N, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+      s = cuda_status(e);
+      goto fail;
+    }
+  }
+  P->n_out = 1;
+  P->info.N_dft = b.N; P->info.k_lb = bk.k_lb; P->info.k_ub = bk.k_ub; P->info.n_bins = bk.K;
+  P->info.n_x = nx; P->info.n_z = nz; P->info.n_elements = ne; P->info.n_angles = 1; P->info.n_samples = d->n_samples;
+  P->info.f_monotone = mono;
+  P->info.terms = (long long)nx * nz * ne * ne * bk.K;
+  P->info.scale = 2.0 / b.N;
+  *out = P;
+  return FNUM_OK;
+fail:
+  delete P;
+  return s;
+}
+
+int plan_dft(fnum_plan* P, const void* rf, int is_double, cudaStream_t st) {
+  if (P->kind == 0) {
+    const fnum::PWDev& D = P->pw;
+    return cuda_status(fnum::launch_dft_pw(rf, is_double, D.na, D.ne, P->nt, P->tw, P->band.N, D.k_lb, D.K, P->X, st));
+  }
+  const fnum::SADev& D = P->sa;
+  return cuda_status(fnum::launch_dft_sa(rf, is_double, D.ne * D.ne, P->nt, P->tw, P->band.N, D.k_lb, D.K, P->X, st));
+}
+
+int plan_beamform(fnum_plan* P, void* image, float* w, float* w2, cudaStream_t st) {
+  FNUM_CUDA(cudaMemsetAsync(P->counters, 0, 4 * sizeof(unsigned long long), st));
+  const bool plain = (P->flags & FNUM_FLAG_PLAIN_KERNEL) != 0;
+  if (P->kind == 1) {
+    cudaError_t e = plain ? fnum::launch_sa_plain(P->sa, (float2*)image, w, w2, st)
+                          : fnum::launch_sa_fused(P->sa, P->grid, (float2*)image, w, w2, st);
+    return cuda_status(e);
+  }
+  const fnum::PWDev& D = P->pw;
+  if (P->n_out == 1) {
+    cudaError_t e = plain ? fnum::launch_pw_plain(D, (float2*)image, w, st)
+                          : fnum::launch_pw_fused(D, P->grid, (float2*)image, w, st);
+    return cuda_status(e);
+  }
+  for (int a = 0; a < D.na; ++a) {
+    fnum::PWDev Da = D;
+    Da.na = 1;
+    Da.x_a0 = a;
+    Da.tx_ax = D.tx_ax + (size_t)a * D.nx;
+    Da.tx_az = D.tx_az + (size_t)a * D.nz;
+    Da.tx_f = D.tx_f + a;
+    float2* img = (float2*)image + (size_t)a * D.nx * D.nz;
+    float* wa = (a == 0) ? w : nullptr;
+    cudaError_t e = plain ? fnum::launch_pw_plain(Da, img, wa, st) : fnum::launch_pw_fused(Da, P->grid, img, wa, st);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  return FNUM_OK;
+}
+
+// host-buffer execution shared by fnum_das_pw / fnum_das_sa
+int run_host(fnum_plan* P, const double* rf, size_t rf_count, float* re, float* im, float* w, float* w2) {
+  const size_t nvox = (size_t)P->info.n_x * P->info.n_z;
+  const size_t nimg = nvox * P->n_out;
+  double* d_rf = nullptr;
+  float2* d_img = nullptr;
+  float* d_w = nullptr;
+  float* d_w2 = nullptr;
+  int s = FNUM_OK;
+  std::vector<float2> h_img;
+  cudaError_t e = cudaMalloc(&d_rf, rf_count * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&d_img, nimg * sizeof(float2));
+  if (e == cudaSuccess && w) e = cudaMalloc(&d_w, nvox * sizeof(float));
+  if (e == cudaSuccess && w2) e = cudaMalloc(&d_w2, nvox * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemcpy(d_rf, rf, rf_count * sizeof(double), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    s = cuda_status(e);
+    goto done;
+  }
+  if ((s = plan_dft(P, d_rf, 1, 0))) goto done;
+  if ((s = plan_beamform(P, d_img, d_w, d_w2, 0))) goto done;
+  h_img.resize(nimg);
+  e = cudaMemcpy(h_img.data(), d_img, nimg * sizeof(float2), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && w) e = cudaMemcpy(w, d_w, nvox * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && w2) e = cudaMemcpy(w2, d_w2, nvox * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    s = cuda_status(e);
+    goto done;
+  }
+  {
+    unsigned long long c[4];
+    e = cudaMemcpy(c, P->counters, sizeof(c), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+      s = cuda_status(e);
+      goto done;
+    }
+    if (c[2] & fnum::ERR_SEG_OVERFLOW) {
+      s = FNUM_ERR_INTERNAL;
+      goto done;
+    }
+  }
+  for (size_t v = 0; v < nimg; ++v) {
+    re[v] = h_img[v].x;
+    im[v] = h_img[v].y;
+  }
+done:
+  if (d_rf) cudaFree(d_rf);
+  if (d_img) cudaFree(d_img);
+  if (d_w) cudaFree(d_w);
+  if (d_w2) cudaFree(d_w2);
+  (void)cudaGetLastError();
+  return s;
+}
+
+// one cached plan per gateway: repeated calls with the same arguments reuse
+// the device tables (the reference allocates and frees everything per call)
+struct PlanCache {
+  std::mutex mu;
+  std::vector<unsigned char> key;
+  fnum_plan* plan = nullptr;
+};
+PlanCache g_pw_cache, g_sa_cache;
+
+void key_add(std::vector<unsigned char>& k, const void* p, size_t n) {
+  const unsigned char* c = (const unsigned char*)p;
+  k.insert(k.end(), c, c + n);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// exported C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int fnum_abi_version(void) { return FNUM_ABI_VERSION; }
+
+const char* fnum_status_string(int status) {
+  const StatusInfo* e = find_status(status);
+  return e ? e->text : "unknown status";
+}
+
+const char* fnum_status_id(int status, int saft) {
+  const StatusInfo* e = find_status(status);
+  const char* pre = (status == FNUM_ERR_CUDA || status == FNUM_ERR_OUT_OF_MEMORY)
+                        ? "gpu_bf_error_handling"
+                        : (saft ? "gpu_bf_saft_rf" : "gpu_bf_das_pw_rf");
+  snprintf(g_id_buf, sizeof(g_id_buf), "%s:%s", pre, e ? e->id : "Unknown");
+  return g_id_buf;
+}
+
+int fnum_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int fnum_band(const double* positions_z, int n_z, int n_samples, int n_elements, double f_s, double element_width,
+              double element_pitch, double c_0, const double* f_bounds, double index_t0, int* N_dft, int* k_lb,
+              int* k_ub) {
+  if (!positions_z || n_z < 1 || n_samples < 2 || n_elements < 2 || !N_dft || !k_lb || !k_ub) return FNUM_ERR_ARGUMENT;
+  if (!(f_s > 0)) return FNUM_ERR_SAMPLING_RATE;
+  int s = check_array(element_width, element_pitch, c_0);
+  if (s) return s;
+  if ((s = check_band_args(f_s, f_bounds, index_t0))) return s;
+  Band b;
+  if ((s = compute_band(positions_z, n_z, n_samples, n_elements, f_s, element_width, element_pitch, c_0, f_bounds,
+                        index_t0, &b)))
+    return s;
+  *N_dft = b.N;
+  *k_lb = b.k_lb;
+  *k_ub = b.k_ub;
+  return FNUM_OK;
+}
+
+int fnum_f_number_values(const fnum_f_number* f_number, const double* pitch_over_lambda, int n, double* values) {
+  if (!pitch_over_lambda || !values || n < 0) return FNUM_ERR_ARGUMENT;
+  for (int i = 0; i < n; ++i)
+    if (!(pitch_over_lambda[i] > 0)) return FNUM_ERR_ARGUMENT;  // f_number.m:99 mustBePositive
+  return f_number_values(f_number, pitch_over_lambda, n, values);
+}
+
+double fnum_window_value(fnum_window window, double l, double L) { return window_value(window, l, L); }
+
+int fnum_pw_plan_create(const fnum_pw_desc* desc, const double* steering_angles, int n_angles, int flags,
+                        fnum_plan** plan) {
+  if (!plan) return FNUM_ERR_ARGUMENT;
+  *plan = nullptr;
+  return make_pw_plan(desc, steering_angles, n_angles, flags, plan);
+}
+
+int fnum_sa_plan_create(const fnum_sa_desc* desc, int flags, fnum_plan** plan) {
+  if (!plan) return FNUM_ERR_ARGUMENT;
+  *plan = nullptr;
+  return make_sa_plan(desc, flags, plan);
+}
+
+int fnum_plan_execute_dft(fnum_plan* plan, const void* d_rf, int rf_is_double, void* stream) {
+  if (!plan || !d_rf) return FNUM_ERR_ARGUMENT;
+  FNUM_CUDA(cudaSetDevice(plan->device));
+  return plan_dft(plan, d_rf, rf_is_double, (cudaStream_t)stream);
+}
+
+int fnum_plan_execute_beamform(fnum_plan* plan, void* d_image, float* d_weights, float* d_weights_rx, void* stream) {
+  if (!plan || !d_image) return FNUM_ERR_ARGUMENT;
+  FNUM_CUDA(cudaSetDevice(plan->device));
+  return plan_beamform(plan, d_image, d_weights, d_weights_rx, (cudaStream_t)stream);
+}
+
+int fnum_plan_execute(fnum_plan* plan, const void* d_rf, int rf_is_double, void* d_image, float* d_weights,
+                      float* d_weights_rx, void* stream) {
+  if (!plan || !d_rf || !d_image) return FNUM_ERR_ARGUMENT;
+  FNUM_CUDA(cudaSetDevice(plan->device));
+  int s = plan_dft(plan, d_rf, rf_is_double, (cudaStream_t)stream);
+  if (s) return s;
+  return plan_beamform(plan, d_image, d_weights, d_weights_rx, (cudaStream_t)stream);
+}
+
+int fnum_plan_info_get(const fnum_plan* plan, fnum_plan_info* info) {
+  if (!plan || !info) return FNUM_ERR_ARGUMENT;
+  *info = plan->info;
+  unsigned long long c[4] = {0, 0, 0, 0};
+  cudaError_t e = cudaSetDevice(plan->device);
+  if (e == cudaSuccess) e = cudaMemcpy(c, plan->counters, sizeof(c), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return cuda_status(e);
+  }
+  info->active_terms = (long long)c[0];
+  info->zero_weight_bins = (long long)c[1];
+  if (c[2] & fnum::ERR_SEG_OVERFLOW) return FNUM_ERR_INTERNAL;
+  return FNUM_OK;
+}
+
+int fnum_plan_f_numbers(const fnum_plan* plan, double* values) {
+  if (!plan || !values) return FNUM_ERR_ARGUMENT;
+  std::copy(plan->F.begin(), plan->F.end(), values);
+  if (plan->kind == 1) std::copy(plan->F2.begin(), plan->F2.end(), values + plan->F.size());
+  return FNUM_OK;
+}
+
+int fnum_plan_destroy(fnum_plan* plan) {
+  if (!plan) return FNUM_OK;
+  cudaSetDevice(plan->device);
+  delete plan;
+  (void)cudaGetLastError();
+  return FNUM_OK;
+}
+
+int fnum_das_pw(const fnum_pw_desc* desc, const double* steering_angles, int n_angles, const double* data_rf,
+                int flags, float* image_re, float* image_im, float* weights) {
+  if (!desc || !data_rf || !image_re || !image_im) return FNUM_ERR_ARGUMENT;
+  int s = check_pw(desc, steering_angles, n_angles);
+  if (s) return s;
+  // cache key: every input that shapes the plan
+  std::vector<unsigned char> key;
+  key_add(key, desc, sizeof(*desc));
+  key_add(key, desc->positions_x, sizeof(double) * desc->n_x);
+  key_add(key, desc->positions_z, sizeof(double) * desc->n_z);
+  if (desc->f_bounds) key_add(key, desc->f_bounds, 2 * sizeof(double));
+  if (desc->f_number_values) key_add(key, desc->f_number_values, sizeof(double) * desc->n_f_number_values);
+  key_add(key, steering_angles, sizeof(double) * n_angles);
+  key_add(key, &flags, sizeof(flags));
+  std::lock_guard<std::mutex> lock(g_pw_cache.mu);
+  FNUM_CUDA(cudaSetDevice(desc->device));
+  if (!g_pw_cache.plan || g_pw_cache.key != key) {
+    fnum_plan_destroy(g_pw_cache.plan);
+    g_pw_cache.plan = nullptr;
+    g_pw_cache.key.clear();
+    fnum_plan* P = nullptr;
+    if ((s = make_pw_plan(desc, steering_angles, n_angles, flags, &P))) return s;
+    g_pw_cache.plan = P;
+    g_pw_cache.key = key;
+  }
+  const size_t rf_count = (size_t)n_angles * desc->n_elements * desc->n_samples;
+  return run_host(g_pw_cache.plan, data_rf, rf_count, image_re, image_im, weights, nullptr);
+}
+
+int fnum_das_sa(const fnum_sa_desc* desc, const double* data_rf, int flags, float* image_re, float* image_im,
+                float* weights_tx, float* weights_rx) {
+  if (!desc || !data_rf || !image_re || !image_im) return FNUM_ERR_ARGUMENT;
+  int s = check_sa(desc);
+  if (s) return s;
+  std::vector<unsigned char> key;
+  key_add(key, desc, sizeof(*desc));
+  key_add(key, desc->positions_x, sizeof(double) * desc->n_x);
+  key_add(key, desc->positions_z, sizeof(double) * desc->n_z);
+  if (desc->f_bounds) key_add(key, desc->f_bounds, 2 * sizeof(double));
+  if (desc->f_number_tx_values) key_add(key, desc->f_number_tx_values, sizeof(double) * desc->n_f_number_values);
+  if (desc->f_number_rx_values) key_add(key, desc->f_number_rx_values, sizeof(double) * desc->n_f_number_values);
+  key_add(key, &flags, sizeof(flags));
+  std::lock_guard<std::mutex> lock(g_sa_cache.mu);
+  FNUM_CUDA(cudaSetDevice(desc->device));
+  if (!g_sa_cache.plan || g_sa_cache.key != key) {
+    fnum_plan_destroy(g_sa_cache.plan);
+    g_sa_cache.plan = nullptr;
+    g_sa_cache.key.clear();
+    fnum_plan* P = nullptr;
+    if ((s = make_sa_plan(desc, flags, &P))) return s;
+    g_sa_cache.plan = P;
+    g_sa_cache.key = key;
+  }
+  const size_t rf_count = (size_t)desc->n_elements * desc->n_elements * desc->n_samples;
+  return run_host(g_sa_cache.plan, data_rf, rf_count, image_re, image_im, weights_tx, weights_rx);
+}
+
+}  // extern "C"

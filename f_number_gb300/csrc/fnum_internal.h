@@ -1,0 +1,100 @@
+// Internal plan layout shared by the host library (fnum_host.cpp) and the
+// kernels (fnum_kernels.cu).  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fnum {
+
+// double-float numbers are stored as float2 {hi, lo}, value = hi + lo
+typedef float2 dfl;
+
+// block shape of the fused kernels: TILE_X columns x TILE_Z rows of voxels,
+// one voxel per thread, one column per warp
+constexpr int TILE_X = 4;
+constexpr int TILE_Z = 32;
+constexpr int NTHREADS = TILE_X * TILE_Z;
+// band bins per shared-memory spectrum chunk; flushes happen on chunk edges
+constexpr int KCHUNK = 64;
+
+// one aperture segment of one voxel (bins k_start down to the next entry's
+// k_start + 1 share the same apertures): {k_start, i_lb | (i_ub+1) << 16, invW, W}
+// SAFT uses two int4 per segment: tx then rx.
+
+struct PWDev {
+  int nx, nz, ne, na, K, k_lb, k_ub, N_dft;
+  int window_id; float window_par;
+  int norm;            // 1 = divide each bin by its apodization sum
+  int seg_cap;         // segment entries per voxel
+  int flush_chunks;    // flush Horner accumulators every flush_chunks * KCHUNK bins
+  float scale;         // 2 / N_dft
+  // per column [nx]
+  const dfl* col_u;    // K_u x
+  const dfl* col_p;    // M + x / pitch
+  const dfl* col_m;    // x (m)
+  const int* col_emid; // first element with centre >= x
+  // per row [nz]
+  const dfl* row_u2;   // (K_u z)^2
+  const dfl* row_p;    // z / pitch
+  // per element [ne]
+  const dfl* el_u;     // K_u c_e
+  const dfl* el_m;     // c_e (m)
+  const dfl* el_lb;    // c_e - width/2 (m)
+  const dfl* el_ub;    // c_e + width/2 (m)
+  // per angle
+  const dfl* tx_ax;    // [na][nx]  K_u e_x (x - x_ref) + t0 / N
+  const dfl* tx_az;    // [na][nz]  K_u e_z z
+  // per band bin [K]
+  const dfl* g;        // 1 / (2 F); hi < 0 marks F <= FLT_EPSILON (full aperture)
+  // band spectra [ne][K][x_na]; this launch uses angles x_a0 .. x_a0 + na - 1
+  float2* X;
+  int x_na, x_a0;
+  // scratch: [grid][NTHREADS][seg_cap] int4
+  int4* seg;
+  unsigned long long* counters;   // [0] active terms, [1] zero-weight bins, [2] error bits
+  // the per-voxel FP32 kernel reads the reference's float geometry
+  const float* px_f; const float* pz_f;
+  const float* ctr_f; const float* lb_f; const float* ub_f;
+  const float* F_f;    // [K]
+  const float4* tx_f;  // [na] {e_x, e_z, x_ref, 0}
+  float M_f, pitch_f, coef_f, add_f;
+};
+
+struct SADev {
+  int nx, nz, ne, K, k_lb, k_ub, N_dft;
+  int wtx_id; float wtx_par; int wrx_id; float wrx_par;
+  int norm_tx, norm_rx;   // divide by the tx / rx apodization sums
+  int last_bin_only;      // reference: both normalisations off keep only bin k_ub
+  int seg_cap;
+  int flush_chunks;
+  float scale;
+  const dfl* col_u; const dfl* col_p; const dfl* col_m; const int* col_emid;
+  const dfl* row_u2; const dfl* row_p;
+  const dfl* el_u; const dfl* el_m; const dfl* el_lb; const dfl* el_ub;
+  const dfl* gtx; const dfl* grx;   // [K]
+  float2* X;                        // [ntx][nrx][K]
+  int4* seg;                        // [grid][NTHREADS][seg_cap][2]
+  unsigned long long* counters;
+  const float* px_f; const float* pz_f; const float* ctr_f; const float* lb_f; const float* ub_f;
+  const float* Ftx_f; const float* Frx_f;
+  float M_f, pitch_f, coef_f, add_f;
+};
+
+// error bits in counters[2]
+constexpr unsigned long long ERR_SEG_OVERFLOW = 1ull;
+
+// --- launchers (fnum_kernels.cu) -------------------------------------------
+cudaError_t launch_twiddles(float2* tw, int N, cudaStream_t s);
+// rf [nsig][nt] (float or double) -> X[e][k][a] (pw: sig = a*ne + e) or X[sig][k] (sa)
+cudaError_t launch_dft_pw(const void* rf, int is_double, int na, int ne, int nt, const float2* tw, int N,
+                          int k_lb, int K, float2* X, cudaStream_t s);
+cudaError_t launch_dft_sa(const void* rf, int is_double, int nsig, int nt, const float2* tw, int N, int k_lb,
+                          int K, float2* X, cudaStream_t s);
+int pw_fused_grid(const PWDev& d, int* blocks_per_sm);
+int sa_fused_grid(const SADev& d, int* blocks_per_sm);
+cudaError_t launch_pw_fused(const PWDev& d, int grid, float2* image, float* weights, cudaStream_t s);
+cudaError_t launch_pw_plain(const PWDev& d, float2* image, float* weights, cudaStream_t s);
+cudaError_t launch_sa_fused(const SADev& d, int grid, float2* image, float* wtx, float* wrx, cudaStream_t s);
+cudaError_t launch_sa_plain(const SADev& d, float2* image, float* wtx, float* wrx, cudaStream_t s);
+
+}  // namespace fnum

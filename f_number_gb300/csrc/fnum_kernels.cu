@@ -1,0 +1,1001 @@
+// GB300 (sm_103a) kernels of the Fourier-domain delay-and-sum beamformer.
+//
+// Stages (reference counterparts in the f_number project):
+//   twiddles_kernel      table e^{-2 pi i m / N}, m < N (FP64 sincospi, rounded to float)
+//   dft_band_kernel      RF -> band spectra, only bins k_lb..k_ub
+//                        (replaces cufftPlan1d/cufftExecR2C, +cuda/gpu_bf_das_pw_rf.cu:917-925)
+//   pw_fused_kernel      one voxel per thread; replaces das_kernel_distances_pw,
+//                        das_kernel_phase_shifts, the per-bin cublasCgemm and
+//                        das_kernel_normalization (+cuda/gpu_bf_das_pw_rf.cu:965-1057)
+//   sa_fused_kernel      the same for synthetic-aperture data
+//                        (+cuda/gpu_bf_saft_rf.cu:1144-1201, saft_kernel_phase_shifts.cu)
+//   pw_plain_kernel / sa_plain_kernel
+//                        one voxel per thread with the reference's FP32 arithmetic per term
+//                        (__sincosf, float geometry): the plain drop-in baseline.
+//
+// Fused-kernel algorithm.  For a voxel v the image is
+//   I(v) = (2/N) sum_k (1/W_k) sum_e a_{e,k} X_e(k) z_e^k,   z_e = e^{j 2 pi u_e},
+// u_e = (d_tx + d_rx,e) f_s / (N c) + t0 / N in cycles per bin.  The apertures
+// (and so a_{e,k} and W_k) change only at a few "segment" boundaries along k,
+// computed once per voxel and kept in scratch.  Per element the sum over k is
+// a Horner recurrence run from the top bin down:  A <- A z + X_k  (4 FMA per
+// term).  At a boundary where the weight b = a/W changes from b_old to b_new
+// the accumulator is rescaled by b_old / b_new; it is flushed (multiplied by
+// b e^{j 2 pi k u} and added to the voxel) every flush_chunks * KCHUNK bins to
+// bound the phase drift of the recurrence.  u_e is formed in double-float
+// arithmetic and every exponential e^{j 2 pi k u} is reduced exactly to
+// [-1/2, 1/2] cycles before sincospif, so FP32 only carries the final phasor.
+#include "fnum_internal.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+
+namespace fnum {
+
+// ---------------------------------------------------------------------------
+// double-float arithmetic (Dekker / Knuth error-free transformations)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ dfl two_sum(float a, float b) {
+  float s = a + b;
+  float bb = s - a;
+  float e = (a - (s - bb)) + (b - bb);
+  return make_float2(s, e);
+}
+__device__ __forceinline__ dfl fast_two_sum(float a, float b) {
+  float s = a + b;
+  float e = b - (s - a);
+  return make_float2(s, e);
+}
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+  dfl s = two_sum(a.x, b.x);
+  float t = s.y + (a.y + b.y);
+  return fast_two_sum(s.x, t);
+}
+__device__ __forceinline__ dfl df_sub(dfl a, dfl b) { return df_add(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ dfl two_prod(float a, float b) {
+  float p = a * b;
+  float e = fmaf(a, b, -p);
+  return make_float2(p, e);
+}
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+  dfl p = two_prod(a.x, b.x);
+  float t = fmaf(a.x, b.y, fmaf(a.y, b.x, p.y));
+  return fast_two_sum(p.x, t);
+}
+__device__ __forceinline__ dfl df_sqr(dfl a) {
+  dfl p = two_prod(a.x, a.x);
+  float t = fmaf(2.0f * a.x, a.y, p.y);
+  return fast_two_sum(p.x, t);
+}
+__device__ __forceinline__ dfl df_sqrt(dfl a) {
+  if (!(a.x > 0.0f)) return make_float2(0.0f, 0.0f);
+  float r = __fsqrt_rn(a.x);
+  dfl r2 = two_prod(r, r);
+  float d = ((a.x - r2.x) - r2.y) + a.y;  // a - r^2, a.x - r2.x exact (Sterbenz)
+  float c = d * (0.5f / r);
+  return fast_two_sum(r, c);
+}
+__device__ __forceinline__ float df_to_f(dfl a) { return a.x + a.y; }
+
+// e^{j 2 pi k u}: k u reduced exactly to [-1/2, 1/2] cycles, sincospif on the
+// leading part, first-order correction with the trailing part.
+__device__ __forceinline__ float2 cis_ku(int k, dfl u) {
+  const float kf = (float)k;
+  dfl p = two_prod(kf, u.x);
+  const float n = rintf(p.x);
+  const float rh = p.x - n;                  // exact
+  const float rl = fmaf(kf, u.y, p.y);
+  dfl r = two_sum(rh, rl);
+  float s, c;
+  sincospif(2.0f * r.x, &s, &c);
+  const float dphi = 6.28318530717958647692f * r.y;
+  return make_float2(fmaf(-dphi, s, c), fmaf(dphi, c, s));
+}
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+// ---------------------------------------------------------------------------
+// windows (+cuda/gpu_bf_windows.cu:15-103; ids as gpu_bf_helper_functions.cu:56-97)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float win_apply(int id, float par, float l_abs, float L) {
+  if (!(l_abs < L)) return 0.0f;
+  const float u = l_abs / L;
+  switch (id) {
+    case 0: return 1.0f;
+    case 1: return 0.5f * (1.0f + cospif(u));
+    case 2: {
+      const float thr = 1.0f - par;
+      return (u <= thr) ? 1.0f : 0.5f * (1.0f + cospif((u - thr) / par));
+    }
+    case 4: return 1.0f - u;
+    default: return 0.0f;
+  }
+}
+
+// receive aperture bounds of one voxel at one bin (das_kernel_phase_shifts.cu:119-154):
+//   left  i_lb = max(ceil(M + (x - z/(2F))/pitch), 0)      (ne = none)
+//   right i_ub = min(floor(M + (x + z/(2F))/pitch), ne-1)  (-1 = none)
+// with xp = M + x/pitch, zp = z/pitch, g = 1/(2F) in double-float.
+__device__ __forceinline__ void aperture(dfl xp, dfl zp, dfl g, int ne, int& ilb, int& iub) {
+  if (g.x < 0.0f) {  // F <= FLT_EPSILON: the whole array
+    ilb = 0;
+    iub = ne - 1;
+    return;
+  }
+  const dfl w = df_mul(zp, g);
+  const dfl tl = df_sub(xp, w);
+  const dfl tr = df_add(xp, w);
+  float cl = ceilf(tl.x);
+  if (cl == tl.x && tl.y > 0.0f) cl += 1.0f;
+  float fr = floorf(tr.x);
+  if (fr == tr.x && tr.y < 0.0f) fr -= 1.0f;
+  cl = fminf(fmaxf(cl, 0.0f), (float)ne);
+  fr = fminf(fmaxf(fr, -1.0f), (float)(ne - 1));
+  ilb = (int)cl;
+  iub = (int)fr;
+}
+
+// half-widths of the left / right aperture
+__device__ __forceinline__ float half_left(const dfl* el_lb, dfl xm, int ilb, int ne) {
+  if (ilb >= ne) return 0.0f;
+  const dfl l = el_lb[ilb];
+  return (xm.x - l.x) + (xm.y - l.y);
+}
+__device__ __forceinline__ float half_right(const dfl* el_ub, dfl xm, int iub) {
+  if (iub < 0) return 0.0f;
+  const dfl u = el_ub[iub];
+  return (u.x - xm.x) + (u.y - xm.y);
+}
+
+// apodization of element e (dx = c_e - x) for aperture (ilb, iub)
+__device__ __forceinline__ float elem_apod(int id, float par, int e, int emid, int ilb, int iub, float dx,
+                                           float Ll, float Lr) {
+  if (e < emid) return (e >= ilb) ? win_apply(id, par, -dx, Ll) : 0.0f;
+  return (e <= iub) ? win_apply(id, par, dx, Lr) : 0.0f;
+}
+
+// sum of the apodization over the aperture (the normaliser of one bin)
+__device__ float aperture_sum(int id, float par, const dfl* el_m, const dfl* el_lb, const dfl* el_ub, dfl xm,
+                              int ne, int emid, int ilb, int iub) {
+  float W = 0.0f;
+  if (ilb < emid) {
+    const float L = half_left(el_lb, xm, ilb, ne);
+    for (int e = ilb; e < emid; ++e) {
+      const dfl c = el_m[e];
+      const float l = (xm.x - c.x) + (xm.y - c.y);
+      W += win_apply(id, par, l, L);
+    }
+  }
+  if (iub >= emid) {
+    const float L = half_right(el_ub, xm, iub);
+    for (int e = emid; e <= iub; ++e) {
+      const dfl c = el_m[e];
+      const float l = (c.x - xm.x) + (c.y - xm.y);
+      W += win_apply(id, par, l, L);
+    }
+  }
+  return W;
+}
+
+__device__ __forceinline__ int seg_code(int ilb, int iub) { return ilb | ((iub + 1) << 16); }
+__device__ __forceinline__ int code_ilb(int c) { return c & 0xffff; }
+__device__ __forceinline__ int code_iub(int c) { return (c >> 16) - 1; }
+
+// ---------------------------------------------------------------------------
+// twiddles and the band DFT
+// ---------------------------------------------------------------------------
+__global__ void twiddles_kernel(float2* tw, int N) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < N) {
+    double s, c;
+    sincospi(2.0 * (double)m / (double)N, &s, &c);
+    tw[m] = make_float2((float)c, (float)(-s));
+  }
+}
+
+// One block per signal.  X[k] = sum_t x(t) e^{-j 2 pi k t / N} for k = k_lb..k_lb+K-1;
+// the twiddle index (k t) mod N is carried exactly in integers.
+constexpr int DFT_THREADS = 256;
+constexpr int DFT_BINS = 4;
+
+template <typename T>
+__global__ void __launch_bounds__(DFT_THREADS)
+dft_band_kernel(const T* __restrict__ rf, int nt, const float2* __restrict__ tw, int N, int k_lb, int K,
+                float2* __restrict__ X, int out_stride_k, int out_stride_sig_hi, int out_stride_sig_lo,
+                int sig_lo_count) {
+  extern __shared__ float sig[];
+  const int s = blockIdx.x;
+  const T* x = rf + (size_t)s * nt;
+  for (int t = threadIdx.x; t < nt; t += DFT_THREADS) sig[t] = (float)x[t];
+  __syncthreads();
+  const int s_hi = s / sig_lo_count, s_lo = s % sig_lo_count;
+  float2* out = X + (size_t)s_hi * out_stride_sig_hi + (size_t)s_lo * out_stride_sig_lo;
+  for (int kb = threadIdx.x * DFT_BINS; kb < K; kb += DFT_THREADS * DFT_BINS) {
+    int kk[DFT_BINS], m[DFT_BINS];
+    float re[DFT_BINS], im[DFT_BINS], re2[DFT_BINS], im2[DFT_BINS];
+#pragma unroll
+    for (int b = 0; b < DFT_BINS; ++b) {
+      kk[b] = min(k_lb + kb + b, k_lb + K - 1);
+      m[b] = 0;
+      re[b] = im[b] = re2[b] = im2[b] = 0.0f;
+    }
+    int t = 0;
+    for (; t + 1 < nt; t += 2) {
+      const float x0 = sig[t], x1 = sig[t + 1];
+#pragma unroll
+      for (int b = 0; b < DFT_BINS; ++b) {
+        const float2 w0 = __ldg(&tw[m[b]]);
+        m[b] += kk[b];
+        if (m[b] >= N) m[b] -= N;
+        const float2 w1 = __ldg(&tw[m[b]]);
+        m[b] += kk[b];
+        if (m[b] >= N) m[b] -= N;
+        re[b] = fmaf(x0, w0.x, re[b]);
+        im[b] = fmaf(x0, w0.y, im[b]);
+        re2[b] = fmaf(x1, w1.x, re2[b]);
+        im2[b] = fmaf(x1, w1.y, im2[b]);
+      }
+    }
+    if (t < nt) {
+      const float x0 = sig[t];
+#pragma unroll
+      for (int b = 0; b < DFT_BINS; ++b) {
+        const float2 w0 = __ldg(&tw[m[b]]);
+        re[b] = fmaf(x0, w0.x, re[b]);
+        im[b] = fmaf(x0, w0.y, im[b]);
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < DFT_BINS; ++b) {
+      if (kb + b < K) out[(size_t)(kb + b) * out_stride_k] = make_float2(re[b] + re2[b], im[b] + im2[b]);
+    }
+  }
+}
+
+cudaError_t launch_twiddles(float2* tw, int N, cudaStream_t s) {
+  twiddles_kernel<<<(N + 255) / 256, 256, 0, s>>>(tw, N);
+  return cudaGetLastError();
+}
+
+static cudaError_t dft_launch(const void* rf, int is_double, int nsig, int nt, const float2* tw, int N, int k_lb,
+                              int K, float2* X, int sk, int shi, int slo, int nlo, cudaStream_t s) {
+  const size_t smem = (size_t)nt * sizeof(float);
+  if (smem > 48 * 1024) {
+    cudaError_t e = is_double ? cudaFuncSetAttribute(dft_band_kernel<double>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                              : cudaFuncSetAttribute(dft_band_kernel<float>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  if (is_double)
+    dft_band_kernel<double><<<nsig, DFT_THREADS, smem, s>>>((const double*)rf, nt, tw, N, k_lb, K, X, sk, shi,
+                                                             slo, nlo);
+  else
+    dft_band_kernel<float><<<nsig, DFT_THREADS, smem, s>>>((const float*)rf, nt, tw, N, k_lb, K, X, sk, shi, slo,
+                                                            nlo);
+  return cudaGetLastError();
+}
+
+// PW: signal s = a * ne + e  ->  X[e][k][a]
+cudaError_t launch_dft_pw(const void* rf, int is_double, int na, int ne, int nt, const float2* tw, int N, int k_lb,
+                          int K, float2* X, cudaStream_t s) {
+  return dft_launch(rf, is_double, na * ne, nt, tw, N, k_lb, K, X, /*k*/ na, /*hi=a*/ 1, /*lo=e*/ K * na, ne, s);
+}
+// SA: signal s = tx * ne + rx  ->  X[s][k]
+cudaError_t launch_dft_sa(const void* rf, int is_double, int nsig, int nt, const float2* tw, int N, int k_lb, int K,
+                          float2* X, cudaStream_t s) {
+  return dft_launch(rf, is_double, nsig, nt, tw, N, k_lb, K, X, 1, 0, K, nsig, s);
+}
+
+// ---------------------------------------------------------------------------
+// fused plane-wave kernel
+// ---------------------------------------------------------------------------
+// Segment pre-pass of one voxel: walks the band from the top bin down and
+// writes one int4 {k_start, code, invW, W} per aperture change.  Also
+// registers, per element, the highest bin at which it is active anywhere in
+// the block (ktop) and the block's element range.
+__device__ int pw_build_segments(const PWDev& d, int ic, int jc, bool valid, int4* seg, int* ktop, int* e_range,
+                                 float& W_top, unsigned long long& n_active, unsigned long long& n_empty) {
+  W_top = 0.0f;
+  if (!valid) return 0;
+  const dfl xp = d.col_p[ic], zp = d.row_p[jc], xm = d.col_m[ic];
+  const int emid = d.col_emid[ic];
+  int nseg = 0, prev = -1, u_lo = d.ne, u_hi = -1;
+  int act = 0;
+  for (int kk = d.K - 1; kk >= 0; --kk) {
+    int ilb, iub;
+    aperture(xp, zp, d.g[kk], d.ne, ilb, iub);
+    const int code = seg_code(ilb, iub);
+    if (code != prev) {
+      const float W = aperture_sum(d.window_id, d.window_par, d.el_m, d.el_lb, d.el_ub, xm, d.ne, emid, ilb, iub);
+      const float invW = (W > 0.0f) ? (d.norm ? 1.0f / W : 1.0f) : 0.0f;
+      if (nseg < d.seg_cap)
+        seg[nseg] = make_int4(kk + d.k_lb, code, __float_as_int(invW), __float_as_int(W));
+      else
+        atomicOr(&d.counters[2], ERR_SEG_OVERFLOW);
+      if (nseg == 0) W_top = W;
+      ++nseg;
+      prev = code;
+      const int lo = min(ilb, emid), hi = max(iub, emid - 1);
+      act = (W > 0.0f) ? max(hi - lo + 1, 0) : 0;
+      if (lo <= hi) {
+        for (int e = lo; e <= hi && e < u_lo; ++e) atomicMax(&ktop[e], kk + d.k_lb);
+        for (int e = max(u_hi + 1, lo); e <= hi; ++e) atomicMax(&ktop[e], kk + d.k_lb);
+        u_lo = min(u_lo, lo);
+        u_hi = max(u_hi, hi);
+      }
+    }
+    if (act > 0) n_active += (unsigned long long)act; else n_empty += 1ull;
+  }
+  if (u_lo <= u_hi) {
+    atomicMin(&e_range[0], u_lo);
+    atomicMax(&e_range[1], u_hi);
+  }
+  return min(nseg, d.seg_cap);
+}
+
+// find the last segment whose k_start >= kt (segments are sorted by k_start, descending)
+__device__ __forceinline__ int seg_find(const int4* seg, int nseg, int kt) {
+  int lo = 0, hi = nseg - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (seg[mid].x >= kt) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <int EPT, int NA>
+__global__ void __launch_bounds__(NTHREADS)
+pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weights, int n_tiles_x,
+                int n_tiles) {
+  constexpr int CH = EPT * NA;
+  constexpr int ROW = (CH + 1) & ~1;
+  __shared__ __align__(16) float2 xs[KCHUNK * ROW];
+  __shared__ int e_range[2];
+  extern __shared__ int ktop[];  // [ne]
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int4* seg = d.seg + ((size_t)blockIdx.x * NTHREADS + tid) * (size_t)d.seg_cap;
+  unsigned long long n_active = 0, n_empty = 0;
+
+  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int i = (tile % n_tiles_x) * TILE_X + warp;
+    const int j = (tile / n_tiles_x) * TILE_Z + lane;
+    const bool valid = (i < d.nx) && (j < d.nz);
+    const int ic = min(i, d.nx - 1), jc = min(j, d.nz - 1);
+
+    for (int e = tid; e < d.ne; e += NTHREADS) ktop[e] = -1;
+    if (tid == 0) {
+      e_range[0] = d.ne;
+      e_range[1] = -1;
+    }
+    __syncthreads();
+    float W_top;
+    const int nseg = pw_build_segments(d, ic, jc, valid, seg, ktop, e_range, W_top, n_active, n_empty);
+    __syncthreads();
+    const int E_lo = e_range[0], E_hi = e_range[1];
+
+    const dfl xm = d.col_m[ic];
+    const dfl xu = d.col_u[ic];
+    const dfl zu2 = d.row_u2[jc];
+    const int emid = d.col_emid[ic];
+    float2 acc = make_float2(0.0f, 0.0f), comp = make_float2(0.0f, 0.0f);  // Kahan
+
+    for (int a0 = 0; a0 < d.na; a0 += NA) {
+      dfl utx[NA];
+#pragma unroll
+      for (int a = 0; a < NA; ++a) {
+        const int aa = min(a0 + a, d.na - 1);
+        utx[a] = df_add(d.tx_ax[(size_t)aa * d.nx + ic], d.tx_az[(size_t)aa * d.nz + jc]);
+      }
+      for (int e0 = E_lo; e0 <= E_hi; e0 += EPT) {
+        int kt = -1;
+#pragma unroll
+        for (int q = 0; q < EPT; ++q)
+          if (e0 + q <= E_hi) kt = max(kt, ktop[e0 + q]);
+        if (kt < d.k_lb) continue;
+
+        float dxq[EPT], b[EPT];
+        dfl u[EPT][NA];
+        float2 z[EPT][NA], A[EPT][NA];
+#pragma unroll
+        for (int q = 0; q < EPT; ++q) {
+          const int e = min(e0 + q, d.ne - 1);
+          const dfl cm = d.el_m[e];
+          dxq[q] = (cm.x - xm.x) + (cm.y - xm.y);
+          const dfl dxu = df_sub(d.el_u[e], xu);
+          const dfl urx = df_sqrt(df_add(df_sqr(dxu), zu2));
+#pragma unroll
+          for (int a = 0; a < NA; ++a) {
+            u[q][a] = df_add(urx, utx[a]);
+            z[q][a] = cis_ku(1, u[q][a]);
+            A[q][a] = make_float2(0.0f, 0.0f);
+          }
+        }
+        // segment cursor at kt
+        int s = 0, nb = -1;
+        int4 cur = make_int4(0, seg_code(d.ne, -1), 0, 0), nxt = cur;
+        if (nseg > 0) {
+          s = seg_find(seg, nseg, kt);
+          cur = seg[s];
+          if (s + 1 < nseg) {
+            nxt = seg[s + 1];
+            nb = nxt.x;
+          }
+        }
+        {
+          const int ilb = code_ilb(cur.y), iub = code_iub(cur.y);
+          const float Ll = half_left(d.el_lb, xm, ilb, d.ne), Lr = half_right(d.el_ub, xm, iub);
+          const float invW = __int_as_float(cur.z);
+#pragma unroll
+          for (int q = 0; q < EPT; ++q) {
+            const int e = e0 + q;
+            b[q] = (e <= E_hi) ? elem_apod(d.window_id, d.window_par, e, emid, ilb, iub, dxq[q], Ll, Lr) * invW : 0.0f;
+          }
+        }
+        float2 part = make_float2(0.0f, 0.0f);
+
+        int kc_hi = kt;
+        while (kc_hi >= d.k_lb) {
+          const int chunk = (kc_hi - d.k_lb) / KCHUNK;
+          const int kc_lo = d.k_lb + chunk * KCHUNK;
+          const int nk = kc_hi - kc_lo + 1;
+          __syncthreads();
+          for (int t = tid; t < nk * CH; t += NTHREADS) {
+            const int kk = t / CH, r = t - kk * CH, q = r / NA, a = r - q * NA;
+            const int e = e0 + q, aa = a0 + a;
+            float2 v = make_float2(0.0f, 0.0f);
+            if (e < d.ne && aa < d.na) v = d.X[((size_t)e * d.K + (kc_lo - d.k_lb + kk)) * d.x_na + d.x_a0 + aa];
+            xs[kk * ROW + r] = v;
+          }
+          __syncthreads();
+          for (int k = kc_hi; k >= kc_lo; --k) {
+            if (k == nb) {
+              // enter segment s+1 at bin k
+              const int pilb = code_ilb(cur.y), piub = code_iub(cur.y);
+              ++s;
+              cur = nxt;
+              nb = -1;
+              if (s + 1 < nseg) {
+                nxt = seg[s + 1];
+                nb = nxt.x;
+              }
+              const int ilb = code_ilb(cur.y), iub = code_iub(cur.y);
+              const float Ll = half_left(d.el_lb, xm, ilb, d.ne), Lr = half_right(d.el_ub, xm, iub);
+              const float invW = __int_as_float(cur.z);
+              (void)pilb;
+              (void)piub;
+#pragma unroll
+              for (int q = 0; q < EPT; ++q) {
+                const int e = e0 + q;
+                const float bn =
+                    (e <= E_hi) ? elem_apod(d.window_id, d.window_par, e, emid, ilb, iub, dxq[q], Ll, Lr) * invW : 0.0f;
+                const float bo = b[q];
+                if (bn != 0.0f && bo != 0.0f) {
+                  const float r = bo / bn;
+#pragma unroll
+                  for (int a = 0; a < NA; ++a) {
+                    A[q][a].x *= r;
+                    A[q][a].y *= r;
+                  }
+                } else {
+                  if (bo != 0.0f) {  // leaves the aperture below k+1: flush at k+1
+#pragma unroll
+                    for (int a = 0; a < NA; ++a) {
+                      const float2 t = cmul(cis_ku(k + 1, u[q][a]), A[q][a]);
+                      part.x = fmaf(bo, t.x, part.x);
+                      part.y = fmaf(bo, t.y, part.y);
+                    }
+                  }
+#pragma unroll
+                  for (int a = 0; a < NA; ++a) A[q][a] = make_float2(0.0f, 0.0f);
+                }
+                b[q] = bn;
+              }
+            }
+            const float2* xr = &xs[(k - kc_lo) * ROW];
+#pragma unroll
+            for (int q = 0; q < EPT; ++q) {
+#pragma unroll
+              for (int a = 0; a < NA; ++a) {
+                const float2 x = xr[q * NA + a];
+                const float2 Aq = A[q][a], zq = z[q][a];
+                A[q][a].x = fmaf(Aq.x, zq.x, fmaf(-Aq.y, zq.y, x.x));
+                A[q][a].y = fmaf(Aq.x, zq.y, fmaf(Aq.y, zq.x, x.y));
+              }
+            }
+          }
+          if (chunk % d.flush_chunks == 0) {
+#pragma unroll
+            for (int q = 0; q < EPT; ++q) {
+              if (b[q] != 0.0f) {
+#pragma unroll
+                for (int a = 0; a < NA; ++a) {
+                  const float2 t = cmul(cis_ku(kc_lo, u[q][a]), A[q][a]);
+                  part.x = fmaf(b[q], t.x, part.x);
+                  part.y = fmaf(b[q], t.y, part.y);
+                }
+              }
+#pragma unroll
+              for (int a = 0; a < NA; ++a) A[q][a] = make_float2(0.0f, 0.0f);
+            }
+          }
+          kc_hi = kc_lo - 1;
+        }
+        // compensated accumulation of this element group's contribution
+        {
+          float y = part.x - comp.x, t = acc.x + y;
+          comp.x = (t - acc.x) - y;
+          acc.x = t;
+          y = part.y - comp.y;
+          t = acc.y + y;
+          comp.y = (t - acc.y) - y;
+          acc.y = t;
+        }
+      }
+    }
+    if (valid) {
+      image[(size_t)ic * d.nz + jc] = make_float2(acc.x * d.scale, acc.y * d.scale);
+      if (weights) weights[(size_t)ic * d.nz + jc] = W_top;
+    }
+    __syncthreads();
+  }
+  // terms are counted per angle
+  n_active *= (unsigned long long)d.na;
+  n_empty *= (unsigned long long)d.na;
+  atomicAdd(&d.counters[0], n_active);
+  atomicAdd(&d.counters[1], n_empty);
+}
+
+static void pw_pick(const PWDev& d, void** fn) {
+  if (d.na >= 11) *fn = (void*)pw_fused_kernel<1, 11>;
+  else if (d.na >= 4) *fn = (void*)pw_fused_kernel<2, 4>;
+  else if (d.na >= 2) *fn = (void*)pw_fused_kernel<4, 2>;
+  else *fn = (void*)pw_fused_kernel<8, 1>;
+}
+
+int pw_fused_grid(const PWDev& d, int* blocks_per_sm) {
+  void* fn;
+  pw_pick(d, &fn);
+  int dev = 0, nsm = 0, bps = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, NTHREADS, (size_t)d.ne * sizeof(int));
+  if (bps < 1) bps = 1;
+  if (blocks_per_sm) *blocks_per_sm = bps;
+  const int tiles = ((d.nx + TILE_X - 1) / TILE_X) * ((d.nz + TILE_Z - 1) / TILE_Z);
+  return tiles < nsm * bps ? tiles : nsm * bps;
+}
+
+cudaError_t launch_pw_fused(const PWDev& d, int grid, float2* image, float* weights, cudaStream_t s) {
+  const int ntx = (d.nx + TILE_X - 1) / TILE_X;
+  const int tiles = ntx * ((d.nz + TILE_Z - 1) / TILE_Z);
+  const size_t smem = (size_t)d.ne * sizeof(int);
+  if (d.na >= 11) pw_fused_kernel<1, 11><<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, tiles);
+  else if (d.na >= 4) pw_fused_kernel<2, 4><<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, tiles);
+  else if (d.na >= 2) pw_fused_kernel<4, 2><<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, tiles);
+  else pw_fused_kernel<8, 1><<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, tiles);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// plain per-voxel plane-wave kernel (reference arithmetic per term)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float ref_window(int id, float par, float l, float L) {
+  // +cuda/gpu_bf_windows.cu with __cosf, as the reference
+  if (fabsf(l) >= L) return 0.0f;
+  switch (id) {
+    case 0: return 1.0f;
+    case 1: return (1.0f + __cosf(3.14159265358979f * l / L)) / 2.0f;
+    case 2: {
+      const float thr = 1.0f - par, ratio = fabsf(l) / L;
+      if (ratio <= thr) return 1.0f;
+      return (1.0f + __cosf(3.14159265358979f * (ratio - thr) / par)) / 2.0f;
+    }
+    case 4: return 1.0f - fabsf(l) / L;
+    default: return 0.0f;
+  }
+}
+
+// per-term apodization exactly as das_kernel_phase_shifts.cu:111-154 (float)
+__device__ __forceinline__ float ref_apod(int id, float par, float F, float x, float z, float dx, const float* lb,
+                                          const float* ub, int ne, float M, float pitch) {
+  if (dx < 0.0f) {
+    int ia = 0;
+    if (F > FLT_EPSILON) ia = (int)fmaxf(ceilf(M + (x - z / (2.0f * F)) / pitch), 0.0f);
+    return (ia < ne) ? ref_window(id, par, dx, x - lb[ia]) : 0.0f;
+  }
+  int ia = ne - 1;
+  if (F > FLT_EPSILON) ia = (int)fminf(floorf(M + (x + z / (2.0f * F)) / pitch), (float)(ne - 1));
+  return (ia >= 0) ? ref_window(id, par, dx, ub[ia] - x) : 0.0f;
+}
+
+__global__ void __launch_bounds__(NTHREADS) pw_plain_kernel(const PWDev d, float2* image, float* weights) {
+  const int i = blockIdx.x * TILE_X + (threadIdx.x >> 5);
+  const int j = blockIdx.y * TILE_Z + (threadIdx.x & 31);
+  if (i >= d.nx || j >= d.nz) return;
+  const float x = d.px_f[i], z = d.pz_f[j];
+  float2 img = make_float2(0.0f, 0.0f);
+  float Wlast = 0.0f;
+  for (int a = 0; a < d.na; ++a) {
+    const float4 t = d.tx_f[a];
+    const float dtx = t.x * (x - t.z) + t.y * z;  // das_kernel_distances_pw.cu:27
+    for (int kk = 0; kk < d.K; ++kk) {
+      const int k = d.k_lb + kk;
+      const float F = d.F_f[kk];
+      float sr = 0.0f, si = 0.0f, W = 0.0f;
+      for (int e = 0; e < d.ne; ++e) {
+        const float dx = d.ctr_f[e] - x;
+        const float drt = dtx + __fsqrt_rn(dx * dx + z * z);
+        const float ap = ref_apod(d.window_id, d.window_par, F, x, z, dx, d.lb_f, d.ub_f, d.ne, d.M_f, d.pitch_f);
+        float sn, cs;
+        __sincosf((float)k * (d.coef_f * drt + d.add_f), &sn, &cs);
+        const float2 X = d.X[((size_t)e * d.K + kk) * d.x_na + d.x_a0 + a];
+        const float pr = ap * cs, pi = ap * sn;
+        sr += pr * X.x - pi * X.y;
+        si += pr * X.y + pi * X.x;
+        W += ap;
+      }
+      if (d.norm) {
+        if (W != 0.0f) {
+          img.x += sr / W;
+          img.y += si / W;
+        }
+      } else {
+        img.x += sr;
+        img.y += si;
+      }
+      Wlast = W;
+    }
+  }
+  image[(size_t)i * d.nz + j] = make_float2(img.x * d.scale, img.y * d.scale);
+  if (weights) weights[(size_t)i * d.nz + j] = Wlast;
+}
+
+cudaError_t launch_pw_plain(const PWDev& d, float2* image, float* weights, cudaStream_t s) {
+  dim3 grid((d.nx + TILE_X - 1) / TILE_X, (d.nz + TILE_Z - 1) / TILE_Z);
+  pw_plain_kernel<<<grid, NTHREADS, 0, s>>>(d, image, weights);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// fused synthetic-aperture kernel
+// ---------------------------------------------------------------------------
+// Segments carry both apertures: seg[2s] = {k_start, tx code, invWtx, Wtx},
+// seg[2s+1] = {k_start, rx code, invWrx, Wrx}.  The weight of pair (t, r) is
+// a_tx(t) a_rx(r) / (Wtx Wrx) with the normalisations that are on.
+__device__ int sa_build_segments(const SADev& d, int ic, int jc, bool valid, int4* seg, int* ktop_tx, int* ktop_rx,
+                                 int* ranges, float& Wtx_top, float& Wrx_top, unsigned long long& n_active,
+                                 unsigned long long& n_empty) {
+  Wtx_top = Wrx_top = 0.0f;
+  if (!valid) return 0;
+  const dfl xp = d.col_p[ic], zp = d.row_p[jc], xm = d.col_m[ic];
+  const int emid = d.col_emid[ic];
+  int nseg = 0, prev_t = -1, prev_r = -1;
+  int t_lo = d.ne, t_hi = -1, r_lo = d.ne, r_hi = -1;
+  long long act = 0;
+  for (int kk = d.K - 1; kk >= 0; --kk) {
+    int tlb, tub, rlb, rub;
+    aperture(xp, zp, d.gtx[kk], d.ne, tlb, tub);
+    aperture(xp, zp, d.grx[kk], d.ne, rlb, rub);
+    const int ct = seg_code(tlb, tub), cr = seg_code(rlb, rub);
+    if (ct != prev_t || cr != prev_r) {
+      const float Wt = aperture_sum(d.wtx_id, d.wtx_par, d.el_m, d.el_lb, d.el_ub, xm, d.ne, emid, tlb, tub);
+      const float Wr = aperture_sum(d.wrx_id, d.wrx_par, d.el_m, d.el_lb, d.el_ub, xm, d.ne, emid, rlb, rub);
+      const float it = (Wt > 0.0f) ? (d.norm_tx ? 1.0f / Wt : 1.0f) : 0.0f;
+      const float ir = (Wr > 0.0f) ? (d.norm_rx ? 1.0f / Wr : 1.0f) : 0.0f;
+      if (nseg < d.seg_cap) {
+        seg[2 * nseg] = make_int4(kk + d.k_lb, ct, __float_as_int(it), __float_as_int(Wt));
+        seg[2 * nseg + 1] = make_int4(kk + d.k_lb, cr, __float_as_int(ir), __float_as_int(Wr));
+      } else {
+        atomicOr(&d.counters[2], ERR_SEG_OVERFLOW);
+      }
+      if (nseg == 0) {
+        Wtx_top = Wt;
+        Wrx_top = Wr;
+      }
+      ++nseg;
+      prev_t = ct;
+      prev_r = cr;
+      const int lo_t = min(tlb, emid), hi_t = max(tub, emid - 1);
+      const int lo_r = min(rlb, emid), hi_r = max(rub, emid - 1);
+      act = (Wt > 0.0f && Wr > 0.0f) ? (long long)max(hi_t - lo_t + 1, 0) * max(hi_r - lo_r + 1, 0) : 0;
+      if (lo_t <= hi_t) {
+        for (int e = lo_t; e <= hi_t && e < t_lo; ++e) atomicMax(&ktop_tx[e], kk + d.k_lb);
+        for (int e = max(t_hi + 1, lo_t); e <= hi_t; ++e) atomicMax(&ktop_tx[e], kk + d.k_lb);
+        t_lo = min(t_lo, lo_t);
+        t_hi = max(t_hi, hi_t);
+      }
+      if (lo_r <= hi_r) {
+        for (int e = lo_r; e <= hi_r && e < r_lo; ++e) atomicMax(&ktop_rx[e], kk + d.k_lb);
+        for (int e = max(r_hi + 1, lo_r); e <= hi_r; ++e) atomicMax(&ktop_rx[e], kk + d.k_lb);
+        r_lo = min(r_lo, lo_r);
+        r_hi = max(r_hi, hi_r);
+      }
+    }
+    if (act > 0) n_active += (unsigned long long)act; else n_empty += 1ull;
+  }
+  if (t_lo <= t_hi) {
+    atomicMin(&ranges[0], t_lo);
+    atomicMax(&ranges[1], t_hi);
+  }
+  if (r_lo <= r_hi) {
+    atomicMin(&ranges[2], r_lo);
+    atomicMax(&ranges[3], r_hi);
+  }
+  return min(nseg, d.seg_cap);
+}
+
+__device__ __forceinline__ int sa_seg_find(const int4* seg, int nseg, int kt) {
+  int lo = 0, hi = nseg - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (seg[2 * mid].x >= kt) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <int EPT>
+__global__ void __launch_bounds__(NTHREADS)
+sa_fused_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ wtx_out, float* __restrict__ wrx_out,
+                int n_tiles_x, int n_tiles, int weights_only) {
+  constexpr int ROW = (EPT + 1) & ~1;
+  __shared__ __align__(16) float2 xs[KCHUNK * ROW];
+  __shared__ int ranges[4];
+  extern __shared__ int ktops[];  // [2][ne]
+  int* ktop_tx = ktops;
+  int* ktop_rx = ktops + d.ne;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int4* seg = d.seg + ((size_t)blockIdx.x * NTHREADS + tid) * (size_t)d.seg_cap * 2;
+  unsigned long long n_active = 0, n_empty = 0;
+
+  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int i = (tile % n_tiles_x) * TILE_X + warp;
+    const int j = (tile / n_tiles_x) * TILE_Z + lane;
+    const bool valid = (i < d.nx) && (j < d.nz);
+    const int ic = min(i, d.nx - 1), jc = min(j, d.nz - 1);
+    for (int e = tid; e < 2 * d.ne; e += NTHREADS) ktops[e] = -1;
+    if (tid == 0) {
+      ranges[0] = ranges[2] = d.ne;
+      ranges[1] = ranges[3] = -1;
+    }
+    __syncthreads();
+    float Wtx_top, Wrx_top;
+    const int nseg = sa_build_segments(d, ic, jc, valid, seg, ktop_tx, ktop_rx, ranges, Wtx_top, Wrx_top, n_active,
+                                       n_empty);
+    __syncthreads();
+    const int T_lo = ranges[0], T_hi = weights_only ? -1 : ranges[1], R_lo = ranges[2], R_hi = ranges[3];
+
+    const dfl xm = d.col_m[ic], xu = d.col_u[ic], zu2 = d.row_u2[jc];
+    const int emid = d.col_emid[ic];
+    float2 acc = make_float2(0.0f, 0.0f), comp = make_float2(0.0f, 0.0f);
+
+    for (int t = T_lo; t <= T_hi; ++t) {
+      const int kt_t = ktop_tx[t];
+      if (kt_t < d.k_lb) continue;
+      const dfl ctm = d.el_m[t];
+      const float dxt = (ctm.x - xm.x) + (ctm.y - xm.y);
+      const dfl utx = df_sqrt(df_add(df_sqr(df_sub(d.el_u[t], xu)), zu2));
+      for (int r0 = R_lo; r0 <= R_hi; r0 += EPT) {
+        int kt = -1;
+#pragma unroll
+        for (int q = 0; q < EPT; ++q)
+          if (r0 + q <= R_hi) kt = max(kt, ktop_rx[r0 + q]);
+        kt = min(kt, kt_t);
+        if (kt < d.k_lb) continue;
+        float dxq[EPT], b[EPT];
+        dfl u[EPT];
+        float2 z[EPT], A[EPT];
+#pragma unroll
+        for (int q = 0; q < EPT; ++q) {
+          const int e = min(r0 + q, d.ne - 1);
+          const dfl cm = d.el_m[e];
+          dxq[q] = (cm.x - xm.x) + (cm.y - xm.y);
+          const dfl urx = df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2));
+          u[q] = df_add(urx, utx);
+          z[q] = cis_ku(1, u[q]);
+          A[q] = make_float2(0.0f, 0.0f);
+        }
+        int s = 0, nb = -1;
+        int4 ct = make_int4(0, seg_code(d.ne, -1), 0, 0), cr = ct, nt_ = ct, nr_ = ct;
+        if (nseg > 0) {
+          s = sa_seg_find(seg, nseg, kt);
+          ct = seg[2 * s];
+          cr = seg[2 * s + 1];
+          if (s + 1 < nseg) {
+            nt_ = seg[2 * s + 2];
+            nr_ = seg[2 * s + 3];
+            nb = nt_.x;
+          }
+        }
+        float atx;
+        {
+          const int tlb = code_ilb(ct.y), tub = code_iub(ct.y), rlb = code_ilb(cr.y), rub = code_iub(cr.y);
+          atx = elem_apod(d.wtx_id, d.wtx_par, t, emid, tlb, tub, dxt, half_left(d.el_lb, xm, tlb, d.ne),
+                          half_right(d.el_ub, xm, tub)) * __int_as_float(ct.z);
+          const float Ll = half_left(d.el_lb, xm, rlb, d.ne), Lr = half_right(d.el_ub, xm, rub);
+          const float ir = __int_as_float(cr.z);
+#pragma unroll
+          for (int q = 0; q < EPT; ++q) {
+            const int e = r0 + q;
+            b[q] = (e <= R_hi) ? atx * elem_apod(d.wrx_id, d.wrx_par, e, emid, rlb, rub, dxq[q], Ll, Lr) * ir : 0.0f;
+          }
+        }
+        float2 part = make_float2(0.0f, 0.0f);
+        int kc_hi = kt;
+        while (kc_hi >= d.k_lb) {
+          const int chunk = (kc_hi - d.k_lb) / KCHUNK;
+          const int kc_lo = d.k_lb + chunk * KCHUNK;
+          const int nk = kc_hi - kc_lo + 1;
+          __syncthreads();
+          for (int x = tid; x < nk * EPT; x += NTHREADS) {
+            const int kk = x / EPT, q = x - kk * EPT;
+            const int e = r0 + q;
+            float2 v = make_float2(0.0f, 0.0f);
+            if (e < d.ne) v = d.X[((size_t)t * d.ne + e) * d.K + (kc_lo - d.k_lb + kk)];
+            xs[kk * ROW + q] = v;
+          }
+          __syncthreads();
+          for (int k = kc_hi; k >= kc_lo; --k) {
+            if (k == nb) {
+              ++s;
+              ct = nt_;
+              cr = nr_;
+              nb = -1;
+              if (s + 1 < nseg) {
+                nt_ = seg[2 * s + 2];
+                nr_ = seg[2 * s + 3];
+                nb = nt_.x;
+              }
+              const int tlb = code_ilb(ct.y), tub = code_iub(ct.y), rlb = code_ilb(cr.y), rub = code_iub(cr.y);
+              const float atn = elem_apod(d.wtx_id, d.wtx_par, t, emid, tlb, tub, dxt, half_left(d.el_lb, xm, tlb, d.ne),
+                                          half_right(d.el_ub, xm, tub)) * __int_as_float(ct.z);
+              const float Ll = half_left(d.el_lb, xm, rlb, d.ne), Lr = half_right(d.el_ub, xm, rub);
+              const float ir = __int_as_float(cr.z);
+#pragma unroll
+              for (int q = 0; q < EPT; ++q) {
+                const int e = r0 + q;
+                const float bn =
+                    (e <= R_hi) ? atn * elem_apod(d.wrx_id, d.wrx_par, e, emid, rlb, rub, dxq[q], Ll, Lr) * ir : 0.0f;
+                const float bo = b[q];
+                if (bn != 0.0f && bo != 0.0f) {
+                  const float r = bo / bn;
+                  A[q].x *= r;
+                  A[q].y *= r;
+                } else {
+                  if (bo != 0.0f) {
+                    const float2 tt = cmul(cis_ku(k + 1, u[q]), A[q]);
+                    part.x = fmaf(bo, tt.x, part.x);
+                    part.y = fmaf(bo, tt.y, part.y);
+                  }
+                  A[q] = make_float2(0.0f, 0.0f);
+                }
+                b[q] = bn;
+              }
+            }
+            const float2* xr = &xs[(k - kc_lo) * ROW];
+#pragma unroll
+            for (int q = 0; q < EPT; ++q) {
+              const float2 x = xr[q];
+              const float2 Aq = A[q], zq = z[q];
+              A[q].x = fmaf(Aq.x, zq.x, fmaf(-Aq.y, zq.y, x.x));
+              A[q].y = fmaf(Aq.x, zq.y, fmaf(Aq.y, zq.x, x.y));
+            }
+          }
+          if (chunk % d.flush_chunks == 0) {
+#pragma unroll
+            for (int q = 0; q < EPT; ++q) {
+              if (b[q] != 0.0f) {
+                const float2 tt = cmul(cis_ku(kc_lo, u[q]), A[q]);
+                part.x = fmaf(b[q], tt.x, part.x);
+                part.y = fmaf(b[q], tt.y, part.y);
+              }
+              A[q] = make_float2(0.0f, 0.0f);
+            }
+          }
+          kc_hi = kc_lo - 1;
+        }
+        float y = part.x - comp.x, tt = acc.x + y;
+        comp.x = (tt - acc.x) - y;
+        acc.x = tt;
+        y = part.y - comp.y;
+        tt = acc.y + y;
+        comp.y = (tt - acc.y) - y;
+        acc.y = tt;
+      }
+    }
+    if (valid) {
+      image[(size_t)ic * d.nz + jc] = make_float2(acc.x * d.scale, acc.y * d.scale);
+      if (wtx_out) wtx_out[(size_t)ic * d.nz + jc] = Wtx_top;
+      if (wrx_out) wrx_out[(size_t)ic * d.nz + jc] = Wrx_top;
+    }
+    __syncthreads();
+  }
+  atomicAdd(&d.counters[0], n_active);
+  atomicAdd(&d.counters[1], n_empty);
+}
+
+constexpr int SA_EPT = 8;
+
+int sa_fused_grid(const SADev& d, int* blocks_per_sm) {
+  int dev = 0, nsm = 0, bps = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, sa_fused_kernel<SA_EPT>, NTHREADS, (size_t)2 * d.ne * sizeof(int));
+  if (bps < 1) bps = 1;
+  if (blocks_per_sm) *blocks_per_sm = bps;
+  const int tiles = ((d.nx + TILE_X - 1) / TILE_X) * ((d.nz + TILE_Z - 1) / TILE_Z);
+  return tiles < nsm * bps ? tiles : nsm * bps;
+}
+
+cudaError_t launch_sa_fused(const SADev& d, int grid, float2* image, float* wtx, float* wrx, cudaStream_t s) {
+  const int ntx = (d.nx + TILE_X - 1) / TILE_X;
+  const int tiles = ntx * ((d.nz + TILE_Z - 1) / TILE_Z);
+  sa_fused_kernel<SA_EPT><<<grid, NTHREADS, (size_t)2 * d.ne * sizeof(int), s>>>(d, image, wtx, wrx, ntx, tiles,
+                                                                                 d.last_bin_only < 0 ? 1 : 0);
+  return cudaGetLastError();
+}
+
+// plain per-voxel SAFT kernel: saft_kernel_phase_shifts.cu arithmetic per term
+__global__ void __launch_bounds__(NTHREADS) sa_plain_kernel(const SADev d, float2* image, float* wtx_out,
+                                                            float* wrx_out) {
+  const int i = blockIdx.x * TILE_X + (threadIdx.x >> 5);
+  const int j = blockIdx.y * TILE_Z + (threadIdx.x & 31);
+  if (i >= d.nx || j >= d.nz) return;
+  const float x = d.px_f[i], z = d.pz_f[j];
+  float2 img = make_float2(0.0f, 0.0f);
+  float Wt_last = 0.0f, Wr_last = 0.0f;
+  for (int kk = 0; kk < d.K; ++kk) {
+    const int k = d.k_lb + kk;
+    const float Ft = d.Ftx_f[kk], Fr = d.Frx_f[kk];
+    float sr = 0.0f, si = 0.0f, Wt = 0.0f, Wr = 0.0f;
+    for (int t = 0; t < d.ne; ++t) {
+      const float dxt = d.ctr_f[t] - x;  // das_kernel_distances_sw.cu:26-28 with z_tx = 0
+      const float dtx = __fsqrt_rn(dxt * dxt + z * z);
+      const float at = ref_apod(d.wtx_id, d.wtx_par, Ft, x, z, dxt, d.lb_f, d.ub_f, d.ne, d.M_f, d.pitch_f);
+      Wt += at;
+      for (int r = 0; r < d.ne; ++r) {
+        const float dx = d.ctr_f[r] - x;
+        const float drt = dtx + __fsqrt_rn(dx * dx + z * z);
+        const float ar = ref_apod(d.wrx_id, d.wrx_par, Fr, x, z, dx, d.lb_f, d.ub_f, d.ne, d.M_f, d.pitch_f);
+        if (t == 0) Wr += ar;
+        float sn, cs;
+        __sincosf((float)k * (d.coef_f * drt + d.add_f), &sn, &cs);
+        const float2 X = d.X[((size_t)t * d.ne + r) * d.K + kk];
+        const float pr = at * ar * cs, pi = at * ar * sn;
+        sr += pr * X.x - pi * X.y;
+        si += pr * X.y + pi * X.x;
+      }
+    }
+    float den = 1.0f;
+    if (d.norm_rx) den *= Wr;
+    if (d.norm_tx) den *= Wt;
+    if (d.last_bin_only > 0) {
+      if (kk == d.K - 1) {
+        img.x = sr;
+        img.y = si;
+      }
+    } else if (den != 0.0f) {
+      img.x += sr / den;
+      img.y += si / den;
+    }
+    Wt_last = Wt;
+    Wr_last = Wr;
+  }
+  if (d.last_bin_only < 0) img = make_float2(0.0f, 0.0f);
+  image[(size_t)i * d.nz + j] = make_float2(img.x * d.scale, img.y * d.scale);
+  if (wtx_out) wtx_out[(size_t)i * d.nz + j] = Wt_last;
+  if (wrx_out) wrx_out[(size_t)i * d.nz + j] = Wr_last;
+}
+
+cudaError_t launch_sa_plain(const SADev& d, float2* image, float* wtx, float* wrx, cudaStream_t s) {
+  dim3 grid((d.nx + TILE_X - 1) / TILE_X, (d.nz + TILE_Z - 1) / TILE_Z);
+  sa_plain_kernel<<<grid, NTHREADS, 0, s>>>(d, image, wtx, wrx);
+  return cudaGetLastError();
+}
+
+}  // namespace fnum

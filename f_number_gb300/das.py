@@ -1,0 +1,513 @@
+"""Entry points with the reference's signatures.
+
+* ``das_pw`` / ``das_sa`` follow ``das_pw.m`` / ``das_sa.m``: same positional
+  arguments, defaults, validation order and error identifiers
+  (``das_pw.m:85-290``, ``das_sa.m:85-277``), then the ``platforms.gpu``
+  dispatch (``das_pw.m:296-300``, ``das_sa.m:283-287``).
+* ``gpu_bf_das_pw_rf`` / ``gpu_bf_saft_rf`` follow the MEX gateways: their
+  argument lists, MEX defaults (boxcar window, ``angle_lb(70, 1.5, 10)``) and
+  outputs (image, weights).
+* ``PWPlan`` / ``SAPlan`` keep geometry, band tables and scratch resident on
+  the device for repeated, stream-ordered execution on device buffers.
+
+Arrays use MATLAB orientation: ``data_RF`` is [N_t, N_el] (PW) or
+[N_t, N_rx, N_tx] (SA); images are [N_z, N_x].
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _lib
+from . import f_numbers as _fn
+from . import normalizations as _norm
+from . import platforms as _plat
+from . import windows as _win
+from ._lib import FNumError
+
+EPS = float(np.finfo(np.float64).eps)
+DBL_MIN = float(np.finfo(np.float64).tiny)
+
+
+# ---------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------
+def _is_num(x):
+    return isinstance(x, (int, float, np.integer, np.floating)) or (
+        isinstance(x, np.ndarray) and np.issubdtype(x.dtype, np.number))
+
+
+def _real_row(x):
+    a = np.asarray(x)
+    return np.issubdtype(a.dtype, np.number) and not np.iscomplexobj(a) and a.ndim <= 2 and (
+        a.ndim < 2 or a.shape[0] == 1)
+
+
+def _scalar(x):
+    a = np.asarray(x)
+    return np.issubdtype(a.dtype, np.number) and not np.iscomplexobj(a) and a.size == 1
+
+
+def _err(ident, msg):
+    raise FNumError(ident, msg)
+
+
+def _f_number_args(F_number, band_p_over_lambda):
+    """Native classes go to the library as a spec; any other object with a
+    ``compute_values`` method is evaluated here on the band (as the MEX does
+    through mexCallMATLAB, ``+cuda/gpu_bf_helper_functions.cu:35-51``)."""
+    if F_number is None:
+        return _lib.FNumber(_lib.F_DEFAULT, 0, (0.0, 0.0, 0.0)), None
+    try:
+        return F_number.c_struct(), None
+    except (AttributeError, NotImplementedError):
+        vals = np.ascontiguousarray(np.asarray(F_number.compute_values(band_p_over_lambda), dtype=np.float64).ravel())
+        return _lib.FNumber(_lib.F_DEFAULT, 0, (0.0, 0.0, 0.0)), vals
+
+
+def _window_struct(w, ident):
+    if w is None:
+        return _lib.Window(_lib.WINDOW_BOXCAR, 0.0)
+    if not isinstance(w, _win.window):
+        _err(ident, "Window must be a single object of the class windows.window!")
+    return w.c_struct()
+
+
+def _norm_code(n, ident):
+    if n is None:
+        return _lib.NORM_ON
+    if not isinstance(n, _norm.normalization):
+        _err(ident, "Normalization must be a single object of the class normalizations.normalization!")
+    return n.code
+
+
+def band(positions_z, n_samples, n_elements, f_s, element_width, element_pitch, c_0, f_bounds=None, index_t0=0.0):
+    """(N_dft, k_lb, k_ub) of the MEX gateways (``gpu_bf_das_pw_rf.cu:522-556``)."""
+    pz = np.ascontiguousarray(np.asarray(positions_z, dtype=np.float64).ravel())
+    fb = None if f_bounds is None else np.ascontiguousarray(np.asarray(f_bounds, dtype=np.float64).ravel())
+    N, lb, ub = _lib.C.c_int(), _lib.C.c_int(), _lib.C.c_int()
+    _lib.check(_lib.lib().fnum_band(_lib.dptr(pz), pz.size, int(n_samples), int(n_elements), float(f_s),
+                                    float(element_width), float(element_pitch), float(c_0), _lib.dptr(fb),
+                                    float(index_t0), _lib.C.byref(N), _lib.C.byref(lb), _lib.C.byref(ub)))
+    return N.value, lb.value, ub.value
+
+
+def _band_pl(pz, nt, ne, f_s, width, pitch, c_0, fb, t0):
+    N, k_lb, k_ub = band(pz, nt, ne, f_s, width, pitch, c_0, fb, t0)
+    return pitch * np.arange(k_lb, k_ub + 1) * f_s / (N * c_0)
+
+
+# ---------------------------------------------------------------------------
+# MEX gateways
+# ---------------------------------------------------------------------------
+def gpu_bf_das_pw_rf(positions_x, positions_z, data_RF, f_s, steering_angle, element_width, element_pitch, c_0,
+                     f_bounds=None, index_t0=None, window=None, F_number=None, normalization=None, index_gpu=None,
+                     verbosity=None, *, compound=True, kernel="fused"):
+    """``cuda.gpu_bf_das_pw_rf`` (``+cuda/gpu_bf_das_pw_rf.cu:110``): returns
+    (image [N_z, N_x] complex64 scaled by 2/N_dft, weights [N_z, N_x] float32).
+
+    ``steering_angle`` may hold several angles (same geometry, RF stacked along
+    a third axis [N_t, N_el, N_angles]); with ``compound`` the images are summed
+    into one, else an [N_angles, N_z, N_x] stack is returned.
+    ``kernel="plain"`` selects the per-voxel FP32 kernel with the reference's
+    arithmetic."""
+    ident = "gpu_bf_das_pw_rf"
+    px = np.ascontiguousarray(np.asarray(positions_x, dtype=np.float64).ravel())
+    pz = np.ascontiguousarray(np.asarray(positions_z, dtype=np.float64).ravel())
+    rf = np.asarray(data_RF)
+    if rf.ndim not in (2, 3) or np.iscomplexobj(rf):
+        _err(ident + ":InvalidRFData", "RF data must be a real-valued matrix of type double!")
+    angles = np.ascontiguousarray(np.atleast_1d(np.asarray(steering_angle, dtype=np.float64)).ravel())
+    if rf.ndim == 2:
+        rf = rf[:, :, None]
+    nt, ne, na = rf.shape
+    if na != angles.size:
+        _err(ident + ":InvalidRFData", "RF data must hold one [N_t x N_el] block per steering angle!")
+    # [angle][element][time] memory order
+    rf_c = np.ascontiguousarray(np.transpose(rf, (2, 1, 0)), dtype=np.float64)
+    fb = None if f_bounds is None or np.size(f_bounds) == 0 else np.ascontiguousarray(
+        np.asarray(f_bounds, dtype=np.float64).ravel())
+    if fb is not None and fb.size != 2:
+        _err(ident + ":InvalidFrequencyBounds", "Frequency bounds must be a real-valued vector with two entries of type double!")
+    t0 = 0.0 if index_t0 is None else float(index_t0)
+    if verbosity is not None and not (0 <= int(verbosity) < 4):
+        _err(ident + ":InvalidVerbosityLevel", "Selected verbosity level does not exist!")
+    L = _lib.lib()
+    desc = _lib.PWDesc()
+    desc.positions_x, desc.n_x = _lib.dptr(px), px.size
+    desc.positions_z, desc.n_z = _lib.dptr(pz), pz.size
+    desc.n_samples, desc.n_elements = nt, ne
+    desc.f_s, desc.element_width, desc.element_pitch, desc.c_0 = float(f_s), float(element_width), \
+        float(element_pitch), float(c_0)
+    desc.f_bounds = _lib.dptr(fb)
+    desc.index_t0 = t0
+    desc.window = _window_struct(window, ident + ":InvalidWindow")
+    fvals = None
+    if F_number is not None and not hasattr(F_number, "compute_values"):
+        _err(ident + ":InvalidFNumber", "F-number must be a single object of the class f_numbers.f_number!")
+    try:
+        pl = _band_pl(pz, nt, ne, f_s, element_width, element_pitch, c_0, fb, t0) if F_number is not None else None
+    except FNumError as e:
+        raise FNumError(e.identifier, str(e), e.status)
+    desc.f_number, fvals = _f_number_args(F_number, pl)
+    if fvals is not None:
+        desc.f_number_values, desc.n_f_number_values = _lib.dptr(fvals), fvals.size
+    desc.normalization = _norm_code(normalization, ident + ":InvalidNormalization")
+    desc.device = 0 if index_gpu is None else int(index_gpu)
+    flags = (_lib.FLAG_COMPOUND if compound else 0) | (_lib.FLAG_PLAIN_KERNEL if kernel == "plain" else 0)
+    n_out = 1 if compound else na
+    re = np.empty((n_out, px.size, pz.size), dtype=np.float32)
+    im = np.empty_like(re)
+    w = np.empty((px.size, pz.size), dtype=np.float32)
+    st = L.fnum_das_pw(_lib.C.byref(desc), _lib.dptr(angles), na, _lib.dptr(rf_c), flags, _lib.fptr(re),
+                       _lib.fptr(im), _lib.fptr(w))
+    _lib.check(st)
+    img = (re + 1j * im).astype(np.complex64).transpose(0, 2, 1)
+    return (img[0] if n_out == 1 else img), w.T
+
+
+def gpu_bf_saft_rf(positions_x, positions_z, data_RF, f_s, element_width, element_pitch, c_0, f_bounds=None,
+                   index_t0=None, window_tx=None, window_rx=None, F_number_tx=None, F_number_rx=None,
+                   normalization_tx=None, normalization_rx=None, index_gpu=None, verbosity=None, *,
+                   semantics="reference", kernel="fused"):
+    """``cuda.gpu_bf_saft_rf`` (``+cuda/gpu_bf_saft_rf.cu:107``): returns
+    (image, weights_tx, weights_rx).  ``semantics="intended"`` divides by the
+    sums that are on and always accumulates (the reference keeps only the last
+    bin with both normalisations off and returns zeros with only the receive
+    normalisation on)."""
+    ident = "gpu_bf_saft_rf"
+    px = np.ascontiguousarray(np.asarray(positions_x, dtype=np.float64).ravel())
+    pz = np.ascontiguousarray(np.asarray(positions_z, dtype=np.float64).ravel())
+    rf = np.asarray(data_RF)
+    if rf.ndim != 3 or np.iscomplexobj(rf):
+        _err(ident + ":InvalidRFData", "RF data must be a real-valued array of type double with 3 dimensions!")
+    nt, nrx, ntx = rf.shape
+    if nrx != ntx:
+        _err(ident + ":InvalidRFData", "Size of RF data must be equal along 2nd and 3rd dimensions!")
+    rf_c = np.ascontiguousarray(np.transpose(rf, (2, 1, 0)), dtype=np.float64)  # [tx][rx][t]
+    fb = None if f_bounds is None or np.size(f_bounds) == 0 else np.ascontiguousarray(
+        np.asarray(f_bounds, dtype=np.float64).ravel())
+    t0 = 0.0 if index_t0 is None else float(index_t0)
+    L = _lib.lib()
+    desc = _lib.SADesc()
+    desc.positions_x, desc.n_x = _lib.dptr(px), px.size
+    desc.positions_z, desc.n_z = _lib.dptr(pz), pz.size
+    desc.n_samples, desc.n_elements = nt, nrx
+    desc.f_s, desc.element_width, desc.element_pitch, desc.c_0 = float(f_s), float(element_width), \
+        float(element_pitch), float(c_0)
+    desc.f_bounds = _lib.dptr(fb)
+    desc.index_t0 = t0
+    desc.window_tx = _window_struct(window_tx, ident + ":InvalidWindow")
+    desc.window_rx = _window_struct(window_rx, ident + ":InvalidWindow")
+    pl = None
+    if (F_number_tx is not None) or (F_number_rx is not None):
+        pl = _band_pl(pz, nt, nrx, f_s, element_width, element_pitch, c_0, fb, t0)
+    desc.f_number_tx, ftx = _f_number_args(F_number_tx, pl)
+    desc.f_number_rx, frx = _f_number_args(F_number_rx, pl)
+    if ftx is not None or frx is not None:
+        # a value table replaces both specs: evaluate the native one on the band too
+        if ftx is None:
+            ftx = (F_number_tx.compute_values(pl) if F_number_tx is not None else
+                   _fn.grating.angle_lb(70.0, 1.5, 10.0).compute_values(pl))
+        if frx is None:
+            frx = (F_number_rx.compute_values(pl) if F_number_rx is not None else
+                   _fn.grating.angle_lb(70.0, 1.5, 10.0).compute_values(pl))
+        ftx = np.ascontiguousarray(ftx, dtype=np.float64)
+        frx = np.ascontiguousarray(frx, dtype=np.float64)
+        desc.f_number_tx_values, desc.f_number_rx_values = _lib.dptr(ftx), _lib.dptr(frx)
+        desc.n_f_number_values = ftx.size
+    desc.normalization_tx = _norm_code(normalization_tx, ident + ":InvalidNormalization")
+    desc.normalization_rx = _norm_code(normalization_rx, ident + ":InvalidNormalization")
+    desc.device = 0 if index_gpu is None else int(index_gpu)
+    flags = (_lib.FLAG_SAFT_INTENDED if semantics == "intended" else 0) | (
+        _lib.FLAG_PLAIN_KERNEL if kernel == "plain" else 0)
+    re = np.empty((px.size, pz.size), dtype=np.float32)
+    im = np.empty_like(re)
+    wt = np.empty_like(re)
+    wr = np.empty_like(re)
+    st = L.fnum_das_sa(_lib.C.byref(desc), _lib.dptr(rf_c), flags, _lib.fptr(re), _lib.fptr(im), _lib.fptr(wt),
+                       _lib.fptr(wr))
+    _lib.check(st, saft=True)
+    return (re + 1j * im).astype(np.complex64).T, wt.T, wr.T
+
+
+# ---------------------------------------------------------------------------
+# das_pw.m / das_sa.m
+# ---------------------------------------------------------------------------
+def _check_common_m(fn, positions_x, positions_z, f_s):
+    if not _real_row(positions_x):
+        _err(fn + ":NoNumericAndRealRowVector", "positions_x must be a numeric and real-valued row vector!")
+    if not np.all(np.isfinite(np.asarray(positions_x, dtype=np.float64))):
+        _err(fn + ":NoFiniteXCoordinates", "positions_x must contain finite x-coordinates!")
+    if not _real_row(positions_z):
+        _err(fn + ":NoNumericAndRealRowVector", "positions_z must be a numeric and real-valued row vector!")
+    pz = np.asarray(positions_z, dtype=np.float64)
+    if not (np.all(pz > 0) and np.all(np.isfinite(pz))):
+        _err(fn + ":NoPositiveAndFiniteZCoordinates", "positions_z must contain positive and finite z-coordinates!")
+
+
+def _check_scalar(fn, name, v):
+    if not _scalar(v):
+        _err(fn + ":NoNumericAndRealScalar", "%s must be a numeric and real-valued scalar!" % name)
+    return float(np.asarray(v).ravel()[0])
+
+
+def _check_tail_m(fn, f_s, f_bounds, index_t0):
+    if f_bounds is None or np.size(f_bounds) == 0:
+        f_bounds = [EPS, f_s / 2.0]
+    if not _real_row(f_bounds):
+        _err(fn + ":NoNumericAndRealRowVector", "f_bounds must be a numeric and real-valued row vector!")
+    fb = np.asarray(f_bounds, dtype=np.float64).ravel()
+    if not (fb.size == 2 and fb[0] > 0 and fb[1] > fb[0] and fb[1] <= f_s / 2):
+        _err(fn + ":InvalidFrequencyBounds", "f_bounds must be a strictly monotonic increasing sequence!")
+    if index_t0 is None or np.size(index_t0) == 0:
+        index_t0 = 0
+    t0 = _check_scalar(fn, "index_t0", index_t0)
+    if not (t0 >= 0 and t0 == math.floor(t0)):
+        _err(fn + ":InvalidTimeIndex", "index_t0 must be a nonnegative integer!")
+    return fb, t0
+
+
+def _check_geometry_m(fn, f_s, element_width, element_pitch, c_0):
+    f_s = _check_scalar(fn, "f_s", f_s)
+    if not (f_s > 0 and math.isfinite(f_s)):
+        _err(fn + ":InvalidSamplingRate", "f_s must be positive and finite!")
+    w = _check_scalar(fn, "element_width", element_width)
+    if not (w > 0 and math.isfinite(w)):
+        _err(fn + ":InvalidElementWidth", "element_width must be positive and finite!")
+    p = _check_scalar(fn, "element_pitch", element_pitch)
+    if not (p > w and math.isfinite(p)):
+        _err(fn + ":InvalidElementPitch", "element_pitch must be larger than element_width and finite!")
+    c = _check_scalar(fn, "c_0", c_0)
+    if not (c > 0 and math.isfinite(c)):
+        _err(fn + ":InvalidSpeedOfSound", "c_0 must be positive and finite!")
+    return f_s, w, p, c
+
+
+def das_pw(positions_x, positions_z, data_RF, f_s, steering_angle, element_width, element_pitch, c_0,
+           f_bounds=None, index_t0=None, window=None, F_number=None, normalization=None, platform=None):
+    """Fourier-domain DAS for one steered plane wave (``das_pw.m``).
+
+    Returns the complex image [N_z, N_x] of the ``platforms.gpu`` path (the
+    MEX output: single precision, scaled by 2/N_dft).  Defaults follow
+    ``das_pw.m:207-283`` except ``platform``, which defaults to ``gpu(0)``:
+    this package implements the GPU path, and ``platforms.cpu`` (the
+    reference's MATLAB loop) raises ``das_pw:CPUPathNotProvided``."""
+    fn = "das_pw"
+    _check_common_m(fn, positions_x, positions_z, f_s)
+    rf = np.asarray(data_RF)
+    if not (np.issubdtype(rf.dtype, np.number) and not np.iscomplexobj(rf) and rf.ndim == 2):
+        _err(fn + ":NoNumericAndRealMatrix", "data_RF must be a numeric and real-valued matrix!")
+    if not (rf.shape[0] > 1 and rf.shape[1] > 1):
+        _err(fn + ":NoSamples", "data_RF must contain at least two temporal and two spatial samples!")
+    if not np.all(np.isfinite(rf)):
+        _err(fn + ":NoFiniteRFData", "data_RF must contain finite samples!")
+    f_s_v = _check_scalar(fn, "f_s", f_s)
+    if not (f_s_v > 0 and math.isfinite(f_s_v)):
+        _err(fn + ":InvalidSamplingRate", "f_s must be positive and finite!")
+    th = _check_scalar(fn, "steering_angle", steering_angle)
+    if not (-math.pi / 2 < th < math.pi / 2):
+        _err(fn + ":InvalidSteeringAngle",
+             "steering_angle must be larger than negative pi over two and smaller than pi over two!")
+    f_s_v, w, p, c = _check_geometry_m(fn, f_s, element_width, element_pitch, c_0)
+    fb, t0 = _check_tail_m(fn, f_s_v, f_bounds, index_t0)
+    if window is None or (isinstance(window, (list, tuple, np.ndarray)) and len(window) == 0):
+        window = _win.tukey(0.2)
+    if not isinstance(window, _win.window):
+        _err(fn + ":NoWindow", "window must be scalar windows.window!")
+    if F_number is None:
+        F_number = _fn.grating.angle_lb(60.0, 1.5)
+    if not isinstance(F_number, _fn.f_number):
+        _err(fn + ":NoFNumber", "F_number must be scalar f_numbers.f_number!")
+    if normalization is None:
+        normalization = _norm.on()
+    if not isinstance(normalization, _norm.normalization):
+        _err(fn + ":NoNormalization", "normalization must be scalar normalizations.normalization!")
+    if platform is None:
+        platform = _plat.gpu(0)
+    if not isinstance(platform, _plat.platform):
+        _err(fn + ":NoPlatform", "platform must be scalar platforms.platform!")
+    if not isinstance(platform, _plat.gpu):
+        _err(fn + ":CPUPathNotProvided",
+             "platforms.cpu is the reference's MATLAB implementation; this package provides platforms.gpu")
+    image, _ = gpu_bf_das_pw_rf(positions_x, positions_z, rf, f_s_v, th, w, p, c, fb, t0, window, F_number,
+                                normalization, platform.index)
+    return image
+
+
+def das_sa(positions_x, positions_z, data_RF, f_s, element_width, element_pitch, c_0, f_bounds=None, index_t0=None,
+           window_tx=None, window_rx=None, F_number_tx=None, F_number_rx=None, normalization_tx=None,
+           normalization_rx=None, platform=None):
+    """Fourier-domain DAS for a full synthetic aperture data set (``das_sa.m``);
+    data_RF is [N_t, N_rx, N_tx].  Returns (image, weights_tx, weights_rx) of
+    the GPU path (``das_sa.m:285``).  The receive parameters default to the
+    transmit defaults (``das_sa.m`` defines none for them)."""
+    fn = "das_sa"
+    _check_common_m(fn, positions_x, positions_z, f_s)
+    rf = np.asarray(data_RF)
+    if not (np.issubdtype(rf.dtype, np.number) and not np.iscomplexobj(rf) and rf.ndim == 3):
+        _err(fn + ":NoNumericAndReal3DArray", "data_RF must be a numeric and real-valued 3d array!")
+    if not np.all(np.isfinite(rf)):
+        _err(fn + ":NoFiniteRFData", "data_RF must contain finite samples!")
+    f_s_v, w, p, c = _check_geometry_m(fn, f_s, element_width, element_pitch, c_0)
+    fb, t0 = _check_tail_m(fn, f_s_v, f_bounds, index_t0)
+    window_tx = _win.tukey(0.2) if window_tx is None else window_tx
+    window_rx = _win.tukey(0.2) if window_rx is None else window_rx
+    for wv in (window_tx, window_rx):
+        if not isinstance(wv, _win.window):
+            _err(fn + ":NoWindow", "window must be scalar windows.window!")
+    F_number_tx = _fn.grating.angle_lb(60.0, 1.5) if F_number_tx is None else F_number_tx
+    F_number_rx = _fn.grating.angle_lb(60.0, 1.5) if F_number_rx is None else F_number_rx
+    for fv in (F_number_tx, F_number_rx):
+        if not isinstance(fv, _fn.f_number):
+            _err(fn + ":NoFNumber", "F_number must be scalar f_numbers.f_number!")
+    normalization_tx = _norm.on() if normalization_tx is None else normalization_tx
+    normalization_rx = _norm.on() if normalization_rx is None else normalization_rx
+    for nv in (normalization_tx, normalization_rx):
+        if not isinstance(nv, _norm.normalization):
+            _err(fn + ":NoNormalization", "normalization must be scalar normalizations.normalization!")
+    platform = _plat.gpu(0) if platform is None else platform
+    if not isinstance(platform, _plat.platform):
+        _err(fn + ":NoPlatform", "platform must be scalar platforms.platform!")
+    if not isinstance(platform, _plat.gpu):
+        _err(fn + ":CPUPathNotProvided",
+             "platforms.cpu is the reference's MATLAB implementation; this package provides platforms.gpu")
+    return gpu_bf_saft_rf(positions_x, positions_z, rf, f_s_v, w, p, c, fb, t0, window_tx, window_rx, F_number_tx,
+                          F_number_rx, normalization_tx, normalization_rx, platform.index)
+
+
+# ---------------------------------------------------------------------------
+# device-resident plans
+# ---------------------------------------------------------------------------
+class _Plan:
+    _ptr = None
+    _saft = False
+
+    def info(self) -> dict:
+        inf = _lib.PlanInfo()
+        _lib.check(_lib.lib().fnum_plan_info_get(self._ptr, _lib.C.byref(inf)), self._saft)
+        return {f: getattr(inf, f) for f, _ in _lib.PlanInfo._fields_}
+
+    def f_numbers(self):
+        n = self.n_bins * (2 if self._saft else 1)
+        out = np.empty(n, dtype=np.float64)
+        _lib.check(_lib.lib().fnum_plan_f_numbers(self._ptr, _lib.dptr(out)), self._saft)
+        return out
+
+    def close(self):
+        if self._ptr is not None:
+            _lib.lib().fnum_plan_destroy(self._ptr)
+            self._ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _stream_ptr(stream):
+        if stream is None:
+            import torch
+            stream = torch.cuda.current_stream()
+        return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+
+    def execute(self, rf, out=None, weights=None, weights_rx=None, stream=None):
+        """rf: torch CUDA tensor (float32 or float64), PW [A, E, T] / SA [Tx, Rx, T].
+        Returns the image as a complex64 tensor [n_out, N_x, N_z] (scaled)."""
+        import torch
+        if not rf.is_cuda or not rf.is_contiguous():
+            raise ValueError("rf must be a contiguous CUDA tensor")
+        if rf.dtype not in (torch.float32, torch.float64):
+            raise ValueError("rf must be float32 or float64")
+        if out is None:
+            out = torch.empty((self.n_out, self.n_x, self.n_z), dtype=torch.complex64, device=rf.device)
+        st = _lib.lib().fnum_plan_execute(self._ptr, rf.data_ptr(), int(rf.dtype == torch.float64), out.data_ptr(),
+                                          weights.data_ptr() if weights is not None else None,
+                                          weights_rx.data_ptr() if weights_rx is not None else None,
+                                          self._stream_ptr(stream))
+        _lib.check(st, self._saft)
+        return out
+
+    def execute_dft(self, rf, stream=None):
+        import torch
+        _lib.check(_lib.lib().fnum_plan_execute_dft(self._ptr, rf.data_ptr(), int(rf.dtype == torch.float64),
+                                                    self._stream_ptr(stream)), self._saft)
+
+    def execute_beamform(self, out, weights=None, weights_rx=None, stream=None):
+        _lib.check(_lib.lib().fnum_plan_execute_beamform(
+            self._ptr, out.data_ptr(), weights.data_ptr() if weights is not None else None,
+            weights_rx.data_ptr() if weights_rx is not None else None, self._stream_ptr(stream)), self._saft)
+        return out
+
+
+class PWPlan(_Plan):
+    """Plane-wave plan: one or many steering angles with the same geometry."""
+
+    def __init__(self, positions_x, positions_z, n_samples, n_elements, f_s, steering_angles, element_width,
+                 element_pitch, c_0, f_bounds=None, index_t0=0.0, window=None, F_number=None, normalization=None,
+                 device=0, compound=True, kernel="fused"):
+        self._px = np.ascontiguousarray(np.asarray(positions_x, dtype=np.float64).ravel())
+        self._pz = np.ascontiguousarray(np.asarray(positions_z, dtype=np.float64).ravel())
+        self._angles = np.ascontiguousarray(np.atleast_1d(np.asarray(steering_angles, dtype=np.float64)).ravel())
+        self._fb = None if f_bounds is None else np.ascontiguousarray(np.asarray(f_bounds, dtype=np.float64).ravel())
+        d = _lib.PWDesc()
+        d.positions_x, d.n_x = _lib.dptr(self._px), self._px.size
+        d.positions_z, d.n_z = _lib.dptr(self._pz), self._pz.size
+        d.n_samples, d.n_elements = int(n_samples), int(n_elements)
+        d.f_s, d.element_width, d.element_pitch, d.c_0 = float(f_s), float(element_width), float(element_pitch), \
+            float(c_0)
+        d.f_bounds = _lib.dptr(self._fb)
+        d.index_t0 = float(index_t0)
+        d.window = _window_struct(window, "gpu_bf_das_pw_rf:InvalidWindow")
+        pl = _band_pl(self._pz, n_samples, n_elements, f_s, element_width, element_pitch, c_0, self._fb,
+                      index_t0) if F_number is not None else None
+        d.f_number, self._fvals = _f_number_args(F_number, pl)
+        if self._fvals is not None:
+            d.f_number_values, d.n_f_number_values = _lib.dptr(self._fvals), self._fvals.size
+        d.normalization = _norm_code(normalization, "gpu_bf_das_pw_rf:InvalidNormalization")
+        d.device = int(device)
+        flags = (_lib.FLAG_COMPOUND if compound else 0) | (_lib.FLAG_PLAIN_KERNEL if kernel == "plain" else 0)
+        ptr = _lib.C.c_void_p()
+        _lib.check(_lib.lib().fnum_pw_plan_create(_lib.C.byref(d), _lib.dptr(self._angles), self._angles.size, flags,
+                                                  _lib.C.byref(ptr)))
+        self._ptr = ptr
+        inf = self.info()
+        self.n_x, self.n_z, self.n_bins = inf["n_x"], inf["n_z"], inf["n_bins"]
+        self.n_out = 1 if compound else self._angles.size
+
+
+class SAPlan(_Plan):
+    """Synthetic-aperture plan."""
+    _saft = True
+
+    def __init__(self, positions_x, positions_z, n_samples, n_elements, f_s, element_width, element_pitch, c_0,
+                 f_bounds=None, index_t0=0.0, window_tx=None, window_rx=None, F_number_tx=None, F_number_rx=None,
+                 normalization_tx=None, normalization_rx=None, device=0, semantics="reference", kernel="fused"):
+        self._px = np.ascontiguousarray(np.asarray(positions_x, dtype=np.float64).ravel())
+        self._pz = np.ascontiguousarray(np.asarray(positions_z, dtype=np.float64).ravel())
+        self._fb = None if f_bounds is None else np.ascontiguousarray(np.asarray(f_bounds, dtype=np.float64).ravel())
+        d = _lib.SADesc()
+        d.positions_x, d.n_x = _lib.dptr(self._px), self._px.size
+        d.positions_z, d.n_z = _lib.dptr(self._pz), self._pz.size
+        d.n_samples, d.n_elements = int(n_samples), int(n_elements)
+        d.f_s, d.element_width, d.element_pitch, d.c_0 = float(f_s), float(element_width), float(element_pitch), \
+            float(c_0)
+        d.f_bounds = _lib.dptr(self._fb)
+        d.index_t0 = float(index_t0)
+        d.window_tx = _window_struct(window_tx, "gpu_bf_saft_rf:InvalidWindow")
+        d.window_rx = _window_struct(window_rx, "gpu_bf_saft_rf:InvalidWindow")
+        d.f_number_tx, _ = _f_number_args(F_number_tx, None)
+        d.f_number_rx, _ = _f_number_args(F_number_rx, None)
+        d.normalization_tx = _norm_code(normalization_tx, "gpu_bf_saft_rf:InvalidNormalization")
+        d.normalization_rx = _norm_code(normalization_rx, "gpu_bf_saft_rf:InvalidNormalization")
+        d.device = int(device)
+        flags = (_lib.FLAG_SAFT_INTENDED if semantics == "intended" else 0) | (
+            _lib.FLAG_PLAIN_KERNEL if kernel == "plain" else 0)
+        ptr = _lib.C.c_void_p()
+        _lib.check(_lib.lib().fnum_sa_plan_create(_lib.C.byref(d), flags, _lib.C.byref(ptr)), True)
+        self._ptr = ptr
+        inf = self.info()
+        self.n_x, self.n_z, self.n_bins = inf["n_x"], inf["n_z"], inf["n_bins"]
+        self.n_out = 1

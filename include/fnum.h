@@ -1,0 +1,215 @@
+/*
+ * fnum.h -- C ABI of the GB300 Fourier-domain delay-and-sum beamformer.
+ *
+ * This is the boundary a MATLAB MEX gateway (or any other host) binds to in
+ * place of the reference's CUDA MEX files.  Every entry point takes plain
+ * pointers and sizes; no C++ or torch types appear here.
+ *
+ * Reference interfaces replaced (f_number project):
+ *   fnum_das_pw   <- cuda.gpu_bf_das_pw_rf   (+cuda/gpu_bf_das_pw_rf.cu:110, called from das_pw.m:298)
+ *   fnum_das_sa   <- cuda.gpu_bf_saft_rf     (+cuda/gpu_bf_saft_rf.cu:107, called from das_sa.m:285)
+ *   fnum_band     <- DFT order / band logic  (+cuda/gpu_bf_das_pw_rf.cu:522-556)
+ *   fnum_f_number_values <- f_numbers.f_number.compute_values (+f_numbers/f_number.m:50-114),
+ *                     which the MEX reaches through mexCallMATLAB
+ *                     (+cuda/gpu_bf_helper_functions.cu:35-51)
+ *   fnum_window_value    <- windows (+cuda/gpu_bf_windows.cu:15-103)
+ *   fnum_status_id       <- mexErrMsgIdAndTxt identifiers of both gateways
+ *
+ * Conventions (identical to the MEX gateways):
+ *   positions_x [n_x], positions_z [n_z]           metres, double
+ *   data_rf     PW : [n_elements][n_samples]        (MATLAB data_RF(t, e), time fastest)
+ *               SA : [n_tx][n_rx][n_samples]        (MATLAB data_RF(t, rx, tx))
+ *   images      [n_x][n_z]  (MATLAB N_z x N_x column-major), scaled by 2/N_dft,
+ *               real and imaginary parts in separate planes (mxCOMPLEX single)
+ *   weights     [n_x][n_z]  apodization sum of the highest band bin
+ * Errors are returned as status codes; nothing exits, prints or resets the
+ * device.  fnum_status_id() gives the reference's error identifier.
+ */
+#ifndef FNUM_H
+#define FNUM_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FNUM_ABI_VERSION 1
+
+typedef enum fnum_status {
+  FNUM_OK = 0,
+  FNUM_ERR_NO_DEVICE = 1,          /* gpu_bf_das_pw_rf:NoCUDADevices */
+  FNUM_ERR_INVALID_DEVICE = 2,     /* :InvalidCUDADevice */
+  FNUM_ERR_LATERAL_POSITIONS = 3,  /* :InvalidLateralPositions */
+  FNUM_ERR_AXIAL_POSITIONS = 4,    /* :InvalidAxialPositions */
+  FNUM_ERR_RF_DATA = 5,            /* :InvalidRFData */
+  FNUM_ERR_SAMPLING_RATE = 6,      /* :InvalidSamplingRate */
+  FNUM_ERR_STEERING_ANGLE = 7,     /* :InvalidSteeringAngle */
+  FNUM_ERR_ELEMENT_WIDTH = 8,      /* :InvalidElementWidth */
+  FNUM_ERR_ELEMENT_PITCH = 9,      /* :InvalidElementPitch */
+  FNUM_ERR_SOUND_SPEED = 10,       /* :InvalidSoundSpeed */
+  FNUM_ERR_FREQUENCY_BOUND = 11,   /* :InvalidFrequencyBound  (bounds themselves) */
+  FNUM_ERR_FREQUENCY_BOUNDS = 12,  /* :InvalidFrequencyBounds (resulting bin indices) */
+  FNUM_ERR_TIME_SHIFT = 13,        /* :InvalidTimeShift */
+  FNUM_ERR_WINDOW = 14,            /* :InvalidWindow */
+  FNUM_ERR_F_NUMBER = 15,          /* :InvalidFNumber */
+  FNUM_ERR_NORMALIZATION = 16,     /* :InvalidNormalization */
+  FNUM_ERR_VERBOSITY = 17,         /* :InvalidVerbosityLevel */
+  FNUM_ERR_ARGUMENT = 18,          /* null pointer / size out of range */
+  FNUM_ERR_CUDA = 19,              /* gpu_bf_error_handling:CUDAError */
+  FNUM_ERR_OUT_OF_MEMORY = 20,     /* gpu_bf_error_handling:CUDAError (allocation) */
+  FNUM_ERR_INTERNAL = 21,          /* device-side consistency check failed */
+  FNUM_ERR_TX_F_NUMBER = 22,       /* gpu_bf_saft_rf:InvalidTXFNumber */
+  FNUM_ERR_RX_F_NUMBER = 23        /* gpu_bf_saft_rf:InvalidRXFNumber */
+} fnum_status;
+
+/* window ids follow the MEX mapping (+cuda/gpu_bf_helper_functions.cu:56-97) */
+typedef enum fnum_window_id {
+  FNUM_WINDOW_BOXCAR = 0,
+  FNUM_WINDOW_HANN = 1,
+  FNUM_WINDOW_TUKEY = 2,           /* parameter = fraction_cosine in (0, 1) */
+  FNUM_WINDOW_TRIANGULAR = 4
+} fnum_window_id;
+
+typedef struct fnum_window {
+  int id;
+  double parameter;
+} fnum_window;
+
+typedef enum fnum_normalization {
+  FNUM_NORMALIZATION_OFF = 0,      /* normalizations.off */
+  FNUM_NORMALIZATION_ON = 1,       /* normalizations.on */
+  FNUM_NORMALIZATION_WINDOWED = 2  /* normalizations.windowed: the MEX treats it as "on"
+                                      (+cuda/gpu_bf_das_pw_rf.cu:421-427) */
+} fnum_normalization;
+
+/* F-number classes (+f_numbers/**).  p[] holds the constructor arguments. */
+typedef enum fnum_f_number_kind {
+  FNUM_F_DEFAULT = 0,              /* the MEX default angle_lb(70, 1.5, 10) */
+  FNUM_F_CONSTANT = 1,             /* p[0] = value */
+  FNUM_F_ANGLE_LB = 2,             /* grating.angle_lb: p[0] angle_lb_deg, p[1] F_number_ub, p[2] distance_deg */
+  FNUM_F_DISTANCE_CONSTANT = 3,    /* distance.constant: p[0] distance_deg, p[1] F_number_ub (inf allowed) */
+  FNUM_F_DISTANCE_NONE = 4,        /* distance.none */
+  FNUM_F_DIRECTIVITY = 5,          /* directivity: p[0] width_over_pitch, p[1] attenuation_dB, obliquity */
+  FNUM_F_SZABO = 6                 /* directivity.szabo: p[0] width_over_pitch */
+} fnum_f_number_kind;
+
+typedef enum fnum_obliquity { FNUM_OBLIQUITY_RIGID = 0, FNUM_OBLIQUITY_SOFT = 1 } fnum_obliquity;
+
+typedef struct fnum_f_number {
+  int kind;
+  int obliquity;
+  double p[3];
+} fnum_f_number;
+
+/* flags for fnum_das_pw / fnum_das_sa / plans */
+#define FNUM_FLAG_COMPOUND        0x1  /* PW: sum the images of all angles into one image */
+#define FNUM_FLAG_PLAIN_KERNEL    0x2  /* use the per-voxel FP32 kernel (reference arithmetic) */
+#define FNUM_FLAG_SAFT_INTENDED   0x4  /* SA: divide by whichever sums are on, always accumulate */
+
+/* --- information ------------------------------------------------------ */
+int fnum_abi_version(void);
+const char* fnum_status_string(int status);
+/* reference error identifier, e.g. "gpu_bf_das_pw_rf:InvalidFrequencyBounds";
+   saft != 0 selects the gpu_bf_saft_rf prefix */
+const char* fnum_status_id(int status, int saft);
+int fnum_device_count(void);
+
+/* --- band and parameter objects (host only, no GPU needed) -------------- */
+/* DFT order and band bins exactly as +cuda/gpu_bf_das_pw_rf.cu:522-556.
+   f_bounds may be NULL (default [DBL_MIN, f_s/2]). */
+int fnum_band(const double* positions_z, int n_z, int n_samples, int n_elements, double f_s,
+              double element_width, double element_pitch, double c_0, const double* f_bounds,
+              double index_t0, int* N_dft, int* k_lb, int* k_ub);
+
+/* F per normalised element pitch p/lambda (f_numbers.f_number.compute_values) */
+int fnum_f_number_values(const fnum_f_number* f_number, const double* pitch_over_lambda, int n,
+                         double* values);
+
+/* window value at l relative to half-width L (0 where |l| >= L) */
+double fnum_window_value(fnum_window window, double l, double L);
+
+/* --- plane wave (das_pw) ------------------------------------------------ */
+typedef struct fnum_pw_desc {
+  const double* positions_x; int n_x;
+  const double* positions_z; int n_z;
+  int n_samples; int n_elements;
+  double f_s;
+  double element_width; double element_pitch;
+  double c_0;
+  const double* f_bounds;          /* [2] or NULL */
+  double index_t0;
+  fnum_window window;
+  fnum_f_number f_number;
+  const double* f_number_values;   /* optional: F per band bin (overrides f_number) */
+  int n_f_number_values;
+  int normalization;               /* fnum_normalization */
+  int device;
+} fnum_pw_desc;
+
+/* One call = the reference's gpu_bf_das_pw_rf for each steering angle
+   (n_angles >= 1; data_rf holds n_angles blocks of [n_elements][n_samples]).
+   Outputs: image_re/image_im [n_out][n_x][n_z] with n_out = 1 under
+   FNUM_FLAG_COMPOUND, else n_angles; weights [n_x][n_z] (may be NULL). */
+int fnum_das_pw(const fnum_pw_desc* desc, const double* steering_angles, int n_angles,
+                const double* data_rf, int flags, float* image_re, float* image_im, float* weights);
+
+/* --- synthetic aperture (das_sa) ---------------------------------------- */
+typedef struct fnum_sa_desc {
+  const double* positions_x; int n_x;
+  const double* positions_z; int n_z;
+  int n_samples; int n_elements;   /* n_tx == n_rx == n_elements */
+  double f_s;
+  double element_width; double element_pitch;
+  double c_0;
+  const double* f_bounds;
+  double index_t0;
+  fnum_window window_tx; fnum_window window_rx;
+  fnum_f_number f_number_tx; fnum_f_number f_number_rx;
+  const double* f_number_tx_values; const double* f_number_rx_values; int n_f_number_values;
+  int normalization_tx; int normalization_rx;
+  int device;
+} fnum_sa_desc;
+
+int fnum_das_sa(const fnum_sa_desc* desc, const double* data_rf, int flags, float* image_re,
+                float* image_im, float* weights_tx, float* weights_rx);
+
+/* --- device-resident plans (stream-ordered; inputs and outputs in HBM) --- */
+typedef struct fnum_plan fnum_plan;
+
+typedef struct fnum_plan_info {
+  int N_dft; int k_lb; int k_ub; int n_bins;
+  int n_x; int n_z; int n_elements; int n_angles; int n_samples;
+  int f_monotone;                  /* F non-decreasing over the band */
+  long long terms;                 /* voxel x element(-pair) x bin x angle terms of one execute */
+  long long active_terms;          /* terms with nonzero apodization (counted on device, last execute) */
+  long long zero_weight_bins;      /* (voxel, bin) pairs with zero apodization sum, last execute */
+  long long scratch_bytes;         /* device scratch the plan owns */
+  double scale;                    /* 2 / N_dft */
+} fnum_plan_info;
+
+int fnum_pw_plan_create(const fnum_pw_desc* desc, const double* steering_angles, int n_angles,
+                        int flags, fnum_plan** plan);
+int fnum_sa_plan_create(const fnum_sa_desc* desc, int flags, fnum_plan** plan);
+/* d_rf: device pointer, float (rf_is_double = 0) or double; layout as data_rf.
+   d_image: float2 [n_out][n_x][n_z] (interleaved, scaled); d_weights / d_weights_rx
+   may be NULL.  stream: a cudaStream_t (NULL = legacy default stream). */
+int fnum_plan_execute(fnum_plan* plan, const void* d_rf, int rf_is_double, void* d_image,
+                      float* d_weights, float* d_weights_rx, void* stream);
+/* the band stage alone: d_rf -> d_spectra (plan-internal), for timing */
+int fnum_plan_execute_dft(fnum_plan* plan, const void* d_rf, int rf_is_double, void* stream);
+/* the beamforming stage alone on the spectra of the last fnum_plan_execute_dft */
+int fnum_plan_execute_beamform(fnum_plan* plan, void* d_image, float* d_weights, float* d_weights_rx,
+                               void* stream);
+int fnum_plan_info_get(const fnum_plan* plan, fnum_plan_info* info);
+/* copies the plan's F table (n_bins values; two tables for SA: tx then rx) */
+int fnum_plan_f_numbers(const fnum_plan* plan, double* values);
+int fnum_plan_destroy(fnum_plan* plan);
+
+/* --- diagnostics (no counterpart in the reference) ---------------------- */
+/* sustained FP32 FMA throughput of the device (TFLOP/s, 2 flops per FMA): the
+   roofline denominator of the fused kernels, which are bound by the FP32 pipe */
+int fnum_diag_fp32_peak(int device, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FNUM_H */
