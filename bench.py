@@ -41,17 +41,20 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--grid", type=int, default=512, help="voxels per side (512 = the benchmark grid; smaller "
+                    "sizes keep the same 0.06 mm spacing, for profiling)")
     return ap.parse_args()
 
 
-def workload():
+def workload(grid=512):
     from f_number_gb300 import f_numbers, synth, windows
-    wl = synth.cpwc_11_angles(seed=0)
+    wl = synth.cpwc_11_angles(seed=0, grid=(grid, grid))
     return wl, windows.hann(), f_numbers.grating.angle_lb(60.0, 1.5)
 
 
 def config_of(wl, kernel):
-    return {"workload": "cpwc_11angles_128el_2048smp_512x512_2-7MHz_hann_anglelb60",
+    g = "%dx%d" % (wl.positions_x.size, wl.positions_z.size)
+    return {"workload": "cpwc_11angles_128el_2048smp_%s_2-7MHz_hann_anglelb60" % g,
             "n_angles": int(wl.angles.size), "n_elements": wl.array.n_elements, "n_samples": wl.n_samples,
             "grid": [int(wl.positions_x.size), int(wl.positions_z.size)], "band_hz": list(wl.f_bounds),
             "kernel": kernel, "l2": "flushed between timed steps (512 MB write)", "data": "synthetic seeded RF"}
@@ -150,7 +153,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    wl, win, fn = workload()
+    wl, win, fn = workload(args.grid)
     vals = []
     cb = None
     for _ in range(args.warmup if args.warmup < 1 else 1):
@@ -181,7 +184,7 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    wl, win, fn = workload()
+    wl, win, fn = workload(args.grid)
     plan = das.PWPlan(wl.positions_x, wl.positions_z, wl.n_samples, wl.array.n_elements, wl.f_s, wl.angles,
                       wl.array.width, wl.array.pitch, wl.c, list(wl.f_bounds), 0.0, win, fn, device=local,
                       compound=True, kernel=args.kernel)

@@ -616,6 +616,10 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
   D.X = P->X;
   if ((s = P->alloc(&P->counters, 4))) goto fail;
   D.counters = P->counters;
+  if (cudaMemset(P->counters, 0, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+    s = FNUM_ERR_CUDA;
+    goto fail;
+  }
   {
     int bps = 0;
     P->grid = fnum::pw_fused_grid(D, &bps);
@@ -724,6 +728,10 @@ int make_sa_plan(const fnum_sa_desc* d, int flags, fnum_plan** out) {
   D.X = P->X;
   if ((s = P->alloc(&P->counters, 4))) goto fail;
   D.counters = P->counters;
+  if (cudaMemset(P->counters, 0, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+    s = FNUM_ERR_CUDA;
+    goto fail;
+  }
   {
     int bps = 0;
     P->grid = fnum::sa_fused_grid(D, &bps);
