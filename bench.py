@@ -258,6 +258,7 @@ def run_ours(args):
             "frac": achieved / peak.value if peak.value else None, "traffic": traffic_from_profiles(),
             "kernel": "pw_fused_kernel<1,11>", "work": "8 FLOP per active voxel x element x bin x angle term "
             "(complex MAC); %d active of %d nominal terms" % (info["active_terms"], info["terms"]),
+            "executed_terms": info["executed_terms"],
             "peak_source": "measured FP32 FMA throughput (fnum_diag_fp32_peak); MEASURED_PEAKS.json "
             "holds only HBM and bf16 figures"}
     if rank != 0:

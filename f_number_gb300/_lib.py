@@ -87,6 +87,7 @@ class PlanInfo(C.Structure):
         ("terms", C.c_longlong), ("active_terms", C.c_longlong), ("zero_weight_bins", C.c_longlong),
         ("scratch_bytes", C.c_longlong),
         ("scale", C.c_double),
+        ("executed_terms", C.c_longlong),
     ]
 
 

@@ -614,9 +614,9 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
   if ((s = P->alloc(&P->tw, b.N))) goto fail;
   if ((s = P->alloc(&P->X, (size_t)ne * b.K * na))) goto fail;
   D.X = P->X;
-  if ((s = P->alloc(&P->counters, 4))) goto fail;
+  if ((s = P->alloc(&P->counters, 8))) goto fail;
   D.counters = P->counters;
-  if (cudaMemset(P->counters, 0, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+  if (cudaMemset(P->counters, 0, 8 * sizeof(unsigned long long)) != cudaSuccess) {
     s = FNUM_ERR_CUDA;
     goto fail;
   }
@@ -624,9 +624,9 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
     int bps = 0;
     P->grid = fnum::pw_fused_grid(D, &bps);
     int4* seg;
-    if ((s = P->alloc(&seg, (size_t)P->grid * fnum::NTHREADS * D.seg_cap))) goto fail;
+    if ((s = P->alloc(&seg, (size_t)P->grid * fnum::NTHREADS * D.seg_cap * fnum::PW_SEG_INT4))) goto fail;
     D.seg = seg;
-    P->info.scratch_bytes = (long long)P->grid * fnum::NTHREADS * D.seg_cap * (long long)sizeof(int4);
+    P->info.scratch_bytes = (long long)P->grid * fnum::NTHREADS * D.seg_cap * fnum::PW_SEG_INT4 * (long long)sizeof(int4);
   }
   {
     cudaError_t e = fnum::launch_twiddles(P->tw, b.N, 0);
@@ -726,9 +726,9 @@ int make_sa_plan(const fnum_sa_desc* d, int flags, fnum_plan** out) {
   if ((s = P->alloc(&P->tw, b.N))) goto fail;
   if ((s = P->alloc(&P->X, (size_t)ne * ne * bk.K))) goto fail;
   D.X = P->X;
-  if ((s = P->alloc(&P->counters, 4))) goto fail;
+  if ((s = P->alloc(&P->counters, 8))) goto fail;
   D.counters = P->counters;
-  if (cudaMemset(P->counters, 0, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+  if (cudaMemset(P->counters, 0, 8 * sizeof(unsigned long long)) != cudaSuccess) {
     s = FNUM_ERR_CUDA;
     goto fail;
   }
@@ -736,9 +736,9 @@ int make_sa_plan(const fnum_sa_desc* d, int flags, fnum_plan** out) {
     int bps = 0;
     P->grid = fnum::sa_fused_grid(D, &bps);
     int4* seg;
-    if ((s = P->alloc(&seg, (size_t)P->grid * fnum::NTHREADS * D.seg_cap * 2))) goto fail;
+    if ((s = P->alloc(&seg, (size_t)P->grid * fnum::NTHREADS * D.seg_cap * fnum::SA_SEG_INT4))) goto fail;
     D.seg = seg;
-    P->info.scratch_bytes = (long long)P->grid * fnum::NTHREADS * D.seg_cap * 2 * (long long)sizeof(int4);
+    P->info.scratch_bytes = (long long)P->grid * fnum::NTHREADS * D.seg_cap * fnum::SA_SEG_INT4 * (long long)sizeof(int4);
   }
   {
     cudaError_t e = fnum::launch_twiddles(P->tw, b.N, 0);
@@ -771,7 +771,7 @@ int plan_dft(fnum_plan* P, const void* rf, int is_double, cudaStream_t st) {
 }
 
 int plan_beamform(fnum_plan* P, void* image, float* w, float* w2, cudaStream_t st) {
-  FNUM_CUDA(cudaMemsetAsync(P->counters, 0, 4 * sizeof(unsigned long long), st));
+  FNUM_CUDA(cudaMemsetAsync(P->counters, 0, 8 * sizeof(unsigned long long), st));
   const bool plain = (P->flags & FNUM_FLAG_PLAIN_KERNEL) != 0;
   if (P->kind == 1) {
     cudaError_t e = plain ? fnum::launch_sa_plain(P->sa, (float2*)image, w, w2, st)
@@ -829,7 +829,7 @@ int run_host(fnum_plan* P, const double* rf, size_t rf_count, float* re, float* 
     goto done;
   }
   {
-    unsigned long long c[4];
+    unsigned long long c[8];
     e = cudaMemcpy(c, P->counters, sizeof(c), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) {
       s = cuda_status(e);
@@ -963,7 +963,7 @@ int fnum_plan_execute(fnum_plan* plan, const void* d_rf, int rf_is_double, void*
 int fnum_plan_info_get(const fnum_plan* plan, fnum_plan_info* info) {
   if (!plan || !info) return FNUM_ERR_ARGUMENT;
   *info = plan->info;
-  unsigned long long c[4] = {0, 0, 0, 0};
+  unsigned long long c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   cudaError_t e = cudaSetDevice(plan->device);
   if (e == cudaSuccess) e = cudaMemcpy(c, plan->counters, sizeof(c), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) {
@@ -972,6 +972,7 @@ int fnum_plan_info_get(const fnum_plan* plan, fnum_plan_info* info) {
   }
   info->active_terms = (long long)c[0];
   info->zero_weight_bins = (long long)c[1];
+  info->executed_terms = (long long)c[4];
   if (c[2] & fnum::ERR_SEG_OVERFLOW) return FNUM_ERR_INTERNAL;
   return FNUM_OK;
 }

@@ -18,8 +18,12 @@ constexpr int NTHREADS = TILE_X * TILE_Z;
 constexpr int KCHUNK = 64;
 
 // one aperture segment of one voxel (bins k_start down to the next entry's
-// k_start + 1 share the same apertures): {k_start, i_lb | (i_ub+1) << 16, invW, W}
-// SAFT uses two int4 per segment: tx then rx.
+// k_start + 1 share the same apertures).  Plane wave: one int4
+// {k_start, i_lb | (i_ub+1) << 16, 1/W, ratio of 1/W to the previous segment};
+// SAFT: two int4 {k_start, code, 1/W, W}, tx then rx.  Kernels and the host's
+// scratch allocation both size entries with these constants.
+constexpr int PW_SEG_INT4 = 1;
+constexpr int SA_SEG_INT4 = 2;
 
 struct PWDev {
   int nx, nz, ne, na, K, k_lb, k_ub, N_dft;
@@ -51,7 +55,8 @@ struct PWDev {
   int x_na, x_a0;
   // scratch: [grid][NTHREADS][seg_cap] int4
   int4* seg;
-  unsigned long long* counters;   // [0] active terms, [1] zero-weight bins, [2] error bits
+  unsigned long long* counters;   // [0] active terms, [1] zero-weight bins, [2] error bits,
+                                  // [3] tile counter, [4] executed recurrence steps
   // the per-voxel FP32 kernel reads the reference's float geometry
   const float* px_f; const float* pz_f;
   const float* ctr_f; const float* lb_f; const float* ub_f;

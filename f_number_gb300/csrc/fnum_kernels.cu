@@ -293,32 +293,69 @@ cudaError_t launch_dft_sa(const void* rf, int is_double, int nsig, int nt, const
 // ---------------------------------------------------------------------------
 // fused plane-wave kernel
 // ---------------------------------------------------------------------------
+// Apodization of an element inside its aperture, u = |l| / L in [0, 1).
+// Same windows as win_apply; the cosine is the hardware approximation
+// (absolute error below 4e-7 on [0, pi]), which changes weights by < 1e-6.
+__device__ __forceinline__ float win_fast(int id, float par, float inv_par, float u) {
+  switch (id) {
+    case 0: return 1.0f;
+    case 1: return 0.5f + 0.5f * __cosf(3.14159265358979f * u);
+    case 2: {
+      const float thr = 1.0f - par;
+      return (u <= thr) ? 1.0f : 0.5f + 0.5f * __cosf(3.14159265358979f * (u - thr) * inv_par);
+    }
+    case 4: return 1.0f - u;
+    default: return 0.0f;
+  }
+}
+
+// sum of the apodization over the aperture (the normaliser of one bin)
+__device__ float aperture_sum_fast(const PWDev& d, float inv_par, dfl xm, int emid, int ilb, int iub, float invLl,
+                                   float invLr) {
+  float W = 0.0f;
+  for (int e = ilb; e < emid; ++e) {
+    const dfl c = d.el_m[e];
+    W += win_fast(d.window_id, d.window_par, inv_par, ((xm.x - c.x) + (xm.y - c.y)) * invLl);
+  }
+  for (int e = emid; e <= iub; ++e) {
+    const dfl c = d.el_m[e];
+    W += win_fast(d.window_id, d.window_par, inv_par, ((c.x - xm.x) + (c.y - xm.y)) * invLr);
+  }
+  return W;
+}
+
 // Segment pre-pass of one voxel: walks the band from the top bin down and
-// writes one int4 {k_start, code, invW, W} per aperture change.  Also
-// registers, per element, the highest bin at which it is active anywhere in
-// the block (ktop) and the block's element range.
-__device__ int pw_build_segments(const PWDev& d, int ic, int jc, bool valid, int4* seg, int* ktop, int* e_range,
-                                 float& W_top, unsigned long long& n_active, unsigned long long& n_empty) {
+// writes one int4 per aperture change,
+//   {k_start, i_lb | (i_ub+1) << 16, 1/W, (1/W of the previous segment) / (1/W)}.
+// Also registers, per element, the highest bin at which it is active anywhere
+// in the block (ktop) and the block's element range.
+__device__ int pw_build_segments(const PWDev& d, float inv_par, int ic, int jc, bool valid, int4* seg, int* ktop,
+                                 int* e_range, float& W_top, unsigned long long& n_active,
+                                 unsigned long long& n_empty) {
   W_top = 0.0f;
   if (!valid) return 0;
   const dfl xp = d.col_p[ic], zp = d.row_p[jc], xm = d.col_m[ic];
   const int emid = d.col_emid[ic];
-  int nseg = 0, prev = -1, u_lo = d.ne, u_hi = -1;
-  int act = 0;
+  int nseg = 0, prev = -1, u_lo = d.ne, u_hi = -1, act = 0;
+  float invW_prev = 0.0f;
   for (int kk = d.K - 1; kk >= 0; --kk) {
     int ilb, iub;
     aperture(xp, zp, d.g[kk], d.ne, ilb, iub);
     const int code = seg_code(ilb, iub);
     if (code != prev) {
-      const float W = aperture_sum(d.window_id, d.window_par, d.el_m, d.el_lb, d.el_ub, xm, d.ne, emid, ilb, iub);
+      const float Ll = half_left(d.el_lb, xm, ilb, d.ne), Lr = half_right(d.el_ub, xm, iub);
+      const float invLl = (Ll > 0.0f) ? 1.0f / Ll : 0.0f, invLr = (Lr > 0.0f) ? 1.0f / Lr : 0.0f;
+      const float W = aperture_sum_fast(d, inv_par, xm, emid, ilb, iub, invLl, invLr);
       const float invW = (W > 0.0f) ? (d.norm ? 1.0f / W : 1.0f) : 0.0f;
+      const float wr = (invW > 0.0f) ? invW_prev / invW : 0.0f;
       if (nseg < d.seg_cap)
-        seg[nseg] = make_int4(kk + d.k_lb, code, __float_as_int(invW), __float_as_int(W));
+        seg[nseg] = make_int4(kk + d.k_lb, code, __float_as_int(invW), __float_as_int(wr));
       else
         atomicOr(&d.counters[2], ERR_SEG_OVERFLOW);
       if (nseg == 0) W_top = W;
       ++nseg;
       prev = code;
+      invW_prev = invW;
       const int lo = min(ilb, emid), hi = max(iub, emid - 1);
       act = (W > 0.0f) ? max(hi - lo + 1, 0) : 0;
       if (lo <= hi) {
@@ -337,8 +374,8 @@ __device__ int pw_build_segments(const PWDev& d, int ic, int jc, bool valid, int
   return min(nseg, d.seg_cap);
 }
 
-// find the last segment whose k_start >= kt (segments are sorted by k_start, descending)
-__device__ __forceinline__ int seg_find(const int4* seg, int nseg, int kt) {
+// last segment whose k_start >= kt (entries sorted by k_start, descending)
+__device__ __forceinline__ int seg_find1(const int4* seg, int nseg, int kt) {
   int lo = 0, hi = nseg - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
@@ -347,34 +384,71 @@ __device__ __forceinline__ int seg_find(const int4* seg, int nseg, int kt) {
   return lo;
 }
 
+// tiles are visited deepest rows first (they carry the widest apertures)
+__device__ __forceinline__ void tile_coords(int tile, int n_tiles_x, int n_tiles_z, int& tx, int& tz) {
+  tz = n_tiles_z - 1 - tile / n_tiles_x;
+  tx = tile % n_tiles_x;
+}
+
+// 1 / half-width of the aperture side an element belongs to (edges from shared memory)
+__device__ __forceinline__ float inv_half_width(const dfl* lb_s, const dfl* ub_s, dfl xm, bool left, int ilb, int iub) {
+  float L;
+  if (left) {
+    const dfl l = lb_s[ilb];
+    L = (xm.x - l.x) + (xm.y - l.y);
+  } else {
+    const dfl u = ub_s[iub];
+    L = (u.x - xm.x) + (u.y - xm.y);
+  }
+  return __fdividef(1.0f, L);
+}
+
+constexpr int SEG_RING = 2;  // segment entries prefetched ahead of the recurrence
+
 template <int EPT, int NA>
-__global__ void __launch_bounds__(NTHREADS)
+__global__ void __launch_bounds__(NTHREADS, 4)
 pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weights, int n_tiles_x,
-                int n_tiles) {
+                int n_tiles_z) {
   constexpr int CH = EPT * NA;
   constexpr int ROW = (CH + 1) & ~1;
   __shared__ __align__(16) float2 xs[KCHUNK * ROW];
+  __shared__ dfl utx_s[NA][NTHREADS];
   __shared__ int e_range[2];
-  extern __shared__ int ktop[];  // [ne]
+  __shared__ int s_tile;
+  extern __shared__ __align__(16) unsigned char dyn[];  // lb[ne], ub[ne] (dfl), ktop[ne]
+  dfl* lb_s = (dfl*)dyn;
+  dfl* ub_s = lb_s + d.ne;
+  int* ktop = (int*)(ub_s + d.ne);
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  int4* seg = d.seg + ((size_t)blockIdx.x * NTHREADS + tid) * (size_t)d.seg_cap;
-  unsigned long long n_active = 0, n_empty = 0;
+  const int n_tiles = n_tiles_x * n_tiles_z;
+  int4* seg = d.seg + ((size_t)blockIdx.x * NTHREADS + tid) * (size_t)d.seg_cap * PW_SEG_INT4;
+  const float inv_par = (d.window_par > 0.0f) ? 1.0f / d.window_par : 0.0f;
+  unsigned long long n_active = 0, n_empty = 0, n_exec = 0;
+  for (int e = tid; e < d.ne; e += NTHREADS) {
+    lb_s[e] = d.el_lb[e];
+    ub_s[e] = d.el_ub[e];
+  }
 
-  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-    const int i = (tile % n_tiles_x) * TILE_X + warp;
-    const int j = (tile / n_tiles_x) * TILE_Z + lane;
-    const bool valid = (i < d.nx) && (j < d.nz);
-    const int ic = min(i, d.nx - 1), jc = min(j, d.nz - 1);
-
+  for (;;) {
+    if (tid == 0) s_tile = (int)atomicAdd(&d.counters[3], 1ull);
     for (int e = tid; e < d.ne; e += NTHREADS) ktop[e] = -1;
     if (tid == 0) {
       e_range[0] = d.ne;
       e_range[1] = -1;
     }
     __syncthreads();
+    const int tile = s_tile;
+    if (tile >= n_tiles) break;
+    int tx, tz;
+    tile_coords(tile, n_tiles_x, n_tiles_z, tx, tz);
+    const int i = tx * TILE_X + warp;
+    const int j = tz * TILE_Z + lane;
+    const bool valid = (i < d.nx) && (j < d.nz);
+    const int ic = min(i, d.nx - 1), jc = min(j, d.nz - 1);
+
     float W_top;
-    const int nseg = pw_build_segments(d, ic, jc, valid, seg, ktop, e_range, W_top, n_active, n_empty);
+    const int nseg = pw_build_segments(d, inv_par, ic, jc, valid, seg, ktop, e_range, W_top, n_active, n_empty);
     __syncthreads();
     const int E_lo = e_range[0], E_hi = e_range[1];
 
@@ -385,11 +459,10 @@ pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
     float2 acc = make_float2(0.0f, 0.0f), comp = make_float2(0.0f, 0.0f);  // Kahan
 
     for (int a0 = 0; a0 < d.na; a0 += NA) {
-      dfl utx[NA];
 #pragma unroll
       for (int a = 0; a < NA; ++a) {
         const int aa = min(a0 + a, d.na - 1);
-        utx[a] = df_add(d.tx_ax[(size_t)aa * d.nx + ic], d.tx_az[(size_t)aa * d.nz + jc]);
+        utx_s[a][tid] = df_add(d.tx_ax[(size_t)aa * d.nx + ic], d.tx_az[(size_t)aa * d.nz + jc]);
       }
       for (int e0 = E_lo; e0 <= E_hi; e0 += EPT) {
         int kt = -1;
@@ -397,44 +470,51 @@ pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
         for (int q = 0; q < EPT; ++q)
           if (e0 + q <= E_hi) kt = max(kt, ktop[e0 + q]);
         if (kt < d.k_lb) continue;
+        if (tid == 0) n_exec += (unsigned long long)(kt - d.k_lb + 1) * CH * NTHREADS;
 
-        float dxq[EPT], b[EPT];
-        dfl u[EPT][NA];
+        float dxa[EPT], aw[EPT], b[EPT];
+        dfl urx[EPT];
         float2 z[EPT][NA], A[EPT][NA];
 #pragma unroll
         for (int q = 0; q < EPT; ++q) {
           const int e = min(e0 + q, d.ne - 1);
           const dfl cm = d.el_m[e];
-          dxq[q] = (cm.x - xm.x) + (cm.y - xm.y);
-          const dfl dxu = df_sub(d.el_u[e], xu);
-          const dfl urx = df_sqrt(df_add(df_sqr(dxu), zu2));
+          dxa[q] = fabsf((cm.x - xm.x) + (cm.y - xm.y));
+          urx[q] = df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2));
 #pragma unroll
           for (int a = 0; a < NA; ++a) {
-            u[q][a] = df_add(urx, utx[a]);
-            z[q][a] = cis_ku(1, u[q][a]);
+            z[q][a] = cis_ku(1, df_add(urx[q], utx_s[a][tid]));
             A[q][a] = make_float2(0.0f, 0.0f);
           }
         }
-        // segment cursor at kt
-        int s = 0, nb = -1;
-        int4 cur = make_int4(0, seg_code(d.ne, -1), 0, 0), nxt = cur;
+        // segment cursor at kt and the prefetch ring of the following entries
+        int s = 0, code = seg_code(d.ne, -1);
+        int4 ring[SEG_RING];
+#pragma unroll
+        for (int r = 0; r < SEG_RING; ++r) ring[r] = make_int4(-1, code, 0, 0);
         if (nseg > 0) {
-          s = seg_find(seg, nseg, kt);
-          cur = seg[s];
-          if (s + 1 < nseg) {
-            nxt = seg[s + 1];
-            nb = nxt.x;
-          }
-        }
-        {
-          const int ilb = code_ilb(cur.y), iub = code_iub(cur.y);
-          const float Ll = half_left(d.el_lb, xm, ilb, d.ne), Lr = half_right(d.el_ub, xm, iub);
-          const float invW = __int_as_float(cur.z);
+          s = seg_find1(seg, nseg, kt);
+          const int4 c0 = seg[s];
+          code = c0.y;
+          const int ilb = code_ilb(code), iub = code_iub(code);
+          const int lo = min(ilb, emid), hi = max(iub, emid - 1);
+          const float invW = __int_as_float(c0.z);
 #pragma unroll
           for (int q = 0; q < EPT; ++q) {
             const int e = e0 + q;
-            b[q] = (e <= E_hi) ? elem_apod(d.window_id, d.window_par, e, emid, ilb, iub, dxq[q], Ll, Lr) * invW : 0.0f;
+            const bool left = e < emid;
+            const bool act = (e >= lo) && (e <= hi) && (e <= E_hi);
+            aw[q] = act ? win_fast(d.window_id, d.window_par, inv_par,
+                                   dxa[q] * inv_half_width(lb_s, ub_s, xm, left, ilb, iub))
+                        : 0.0f;
+            b[q] = aw[q] * invW;
           }
+#pragma unroll
+          for (int r = 0; r < SEG_RING; ++r)
+            if (s + 1 + r < nseg) ring[r] = seg[s + 1 + r];
+        } else {
+#pragma unroll
+          for (int q = 0; q < EPT; ++q) aw[q] = b[q] = 0.0f;
         }
         float2 part = make_float2(0.0f, 0.0f);
 
@@ -453,29 +533,36 @@ pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
           }
           __syncthreads();
           for (int k = kc_hi; k >= kc_lo; --k) {
-            if (k == nb) {
-              // enter segment s+1 at bin k
-              const int pilb = code_ilb(cur.y), piub = code_iub(cur.y);
+            if (k == ring[0].x) {
+              // enter the next segment at bin k
+              const int pilb = code_ilb(code), piub = code_iub(code);
+              code = ring[0].y;
+              const float invW = __int_as_float(ring[0].z), wr = __int_as_float(ring[0].w);
+#pragma unroll
+              for (int r = 0; r + 1 < SEG_RING; ++r) ring[r] = ring[r + 1];
               ++s;
-              cur = nxt;
-              nb = -1;
-              if (s + 1 < nseg) {
-                nxt = seg[s + 1];
-                nb = nxt.x;
-              }
-              const int ilb = code_ilb(cur.y), iub = code_iub(cur.y);
-              const float Ll = half_left(d.el_lb, xm, ilb, d.ne), Lr = half_right(d.el_ub, xm, iub);
-              const float invW = __int_as_float(cur.z);
-              (void)pilb;
-              (void)piub;
+              ring[SEG_RING - 1] = (s + SEG_RING < nseg) ? seg[s + SEG_RING] : make_int4(-1, 0, 0, 0);
+              const int ilb = code_ilb(code), iub = code_iub(code);
+              const int lo = min(ilb, emid), hi = max(iub, emid - 1);
 #pragma unroll
               for (int q = 0; q < EPT; ++q) {
                 const int e = e0 + q;
-                const float bn =
-                    (e <= E_hi) ? elem_apod(d.window_id, d.window_par, e, emid, ilb, iub, dxq[q], Ll, Lr) * invW : 0.0f;
+                const bool left = e < emid;
+                const bool act = (e >= lo) && (e <= hi) && (e <= E_hi);
                 const float bo = b[q];
+                float r = wr;
+                if (act) {
+                  if ((left ? (ilb != pilb) : (iub != piub)) || bo == 0.0f) {
+                    const float an = win_fast(d.window_id, d.window_par, inv_par,
+                                              dxa[q] * inv_half_width(lb_s, ub_s, xm, left, ilb, iub));
+                    r = __fdividef(aw[q], an) * wr;
+                    aw[q] = an;
+                  }
+                } else {
+                  aw[q] = 0.0f;
+                }
+                const float bn = aw[q] * invW;
                 if (bn != 0.0f && bo != 0.0f) {
-                  const float r = bo / bn;
 #pragma unroll
                   for (int a = 0; a < NA; ++a) {
                     A[q][a].x *= r;
@@ -485,7 +572,7 @@ pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
                   if (bo != 0.0f) {  // leaves the aperture below k+1: flush at k+1
 #pragma unroll
                     for (int a = 0; a < NA; ++a) {
-                      const float2 t = cmul(cis_ku(k + 1, u[q][a]), A[q][a]);
+                      const float2 t = cmul(cis_ku(k + 1, df_add(urx[q], utx_s[a][tid])), A[q][a]);
                       part.x = fmaf(bo, t.x, part.x);
                       part.y = fmaf(bo, t.y, part.y);
                     }
@@ -514,7 +601,7 @@ pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
               if (b[q] != 0.0f) {
 #pragma unroll
                 for (int a = 0; a < NA; ++a) {
-                  const float2 t = cmul(cis_ku(kc_lo, u[q][a]), A[q][a]);
+                  const float2 t = cmul(cis_ku(kc_lo, df_add(urx[q], utx_s[a][tid])), A[q][a]);
                   part.x = fmaf(b[q], t.x, part.x);
                   part.y = fmaf(b[q], t.y, part.y);
                 }
@@ -548,22 +635,24 @@ pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
   n_empty *= (unsigned long long)d.na;
   atomicAdd(&d.counters[0], n_active);
   atomicAdd(&d.counters[1], n_empty);
+  if (tid == 0) atomicAdd(&d.counters[4], n_exec);
 }
 
-static void pw_pick(const PWDev& d, void** fn) {
-  if (d.na >= 11) *fn = (void*)pw_fused_kernel<1, 11>;
-  else if (d.na >= 4) *fn = (void*)pw_fused_kernel<2, 4>;
-  else if (d.na >= 2) *fn = (void*)pw_fused_kernel<4, 2>;
-  else *fn = (void*)pw_fused_kernel<8, 1>;
+typedef void (*pw_kernel_t)(const PWDev, float2*, float*, int, int);
+
+static pw_kernel_t pw_pick(int na) {
+  if (na >= 11) return pw_fused_kernel<1, 11>;
+  if (na >= 4) return pw_fused_kernel<2, 4>;
+  if (na >= 2) return pw_fused_kernel<2, 2>;
+  return pw_fused_kernel<4, 1>;
 }
 
 int pw_fused_grid(const PWDev& d, int* blocks_per_sm) {
-  void* fn;
-  pw_pick(d, &fn);
+  pw_kernel_t fn = pw_pick(d.na);
   int dev = 0, nsm = 0, bps = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, NTHREADS, (size_t)d.ne * sizeof(int));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, NTHREADS, (size_t)d.ne * (sizeof(int) + 2 * sizeof(dfl)));
   if (bps < 1) bps = 1;
   if (blocks_per_sm) *blocks_per_sm = bps;
   const int tiles = ((d.nx + TILE_X - 1) / TILE_X) * ((d.nz + TILE_Z - 1) / TILE_Z);
@@ -571,16 +660,14 @@ int pw_fused_grid(const PWDev& d, int* blocks_per_sm) {
 }
 
 cudaError_t launch_pw_fused(const PWDev& d, int grid, float2* image, float* weights, cudaStream_t s) {
-  const int ntx = (d.nx + TILE_X - 1) / TILE_X;
-  const int tiles = ntx * ((d.nz + TILE_Z - 1) / TILE_Z);
-  const size_t smem = (size_t)d.ne * sizeof(int);
-  if (d.na >= 11) pw_fused_kernel<1, 11><<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, tiles);
-  else if (d.na >= 4) pw_fused_kernel<2, 4><<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, tiles);
-  else if (d.na >= 2) pw_fused_kernel<4, 2><<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, tiles);
-  else pw_fused_kernel<8, 1><<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, tiles);
+  const int ntx = (d.nx + TILE_X - 1) / TILE_X, ntz = (d.nz + TILE_Z - 1) / TILE_Z;
+  const size_t smem = (size_t)d.ne * (sizeof(int) + 2 * sizeof(dfl));
+  // each launch draws tiles from a fresh counter
+  cudaError_t e = cudaMemsetAsync(d.counters + 3, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  pw_pick(d.na)<<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, ntz);
   return cudaGetLastError();
 }
-
 // ---------------------------------------------------------------------------
 // plain per-voxel plane-wave kernel (reference arithmetic per term)
 // ---------------------------------------------------------------------------
@@ -750,7 +837,7 @@ sa_fused_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
   int* ktop_rx = ktops + d.ne;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  int4* seg = d.seg + ((size_t)blockIdx.x * NTHREADS + tid) * (size_t)d.seg_cap * 2;
+  int4* seg = d.seg + ((size_t)blockIdx.x * NTHREADS + tid) * (size_t)d.seg_cap * SA_SEG_INT4;
   unsigned long long n_active = 0, n_empty = 0;
 
   for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {

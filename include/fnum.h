@@ -184,6 +184,7 @@ typedef struct fnum_plan_info {
   long long zero_weight_bins;      /* (voxel, bin) pairs with zero apodization sum, last execute */
   long long scratch_bytes;         /* device scratch the plan owns */
   double scale;                    /* 2 / N_dft */
+  long long executed_terms;        /* recurrence steps the fused kernel ran (>= active_terms), last execute */
 } fnum_plan_info;
 
 int fnum_pw_plan_create(const fnum_pw_desc* desc, const double* steering_angles, int n_angles,
