@@ -16,12 +16,14 @@ EXPORTS = (
     "fnum_f_number_values", "fnum_window_value", "fnum_das_pw", "fnum_das_sa", "fnum_pw_plan_create",
     "fnum_sa_plan_create", "fnum_plan_execute", "fnum_plan_execute_dft", "fnum_plan_execute_beamform",
     "fnum_plan_info_get", "fnum_plan_f_numbers", "fnum_plan_destroy", "fnum_diag_fp32_peak",
+    "fnum_das_pw_noalloc",
 )
 
 # status codes (fnum_status)
 OK = 0
 ERR_NO_DEVICE = 1
 ERR_INTERNAL = 21
+ERR_NOALLOC_TOO_LARGE = 24
 
 # window ids, normalisations, F-number kinds, flags (fnum.h)
 WINDOW_BOXCAR, WINDOW_HANN, WINDOW_TUKEY, WINDOW_TRIANGULAR = 0, 1, 2, 4
@@ -151,6 +153,9 @@ def lib():
     L.fnum_plan_destroy.argtypes = [C.c_void_p]
     L.fnum_diag_fp32_peak.restype = C.c_int
     L.fnum_diag_fp32_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    L.fnum_das_pw_noalloc.restype = C.c_int
+    L.fnum_das_pw_noalloc.argtypes = [C.POINTER(PWDesc), _dp, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                      C.c_void_p]
     if L.fnum_abi_version() != 1:
         raise LibraryNotBuilt("libfnum.so ABI version mismatch")
     _lib = L

@@ -55,6 +55,8 @@ const StatusInfo kStatus[] = {
     {FNUM_ERR_INTERNAL, "InternalError", "Device-side consistency check failed!"},
     {FNUM_ERR_TX_F_NUMBER, "InvalidTXFNumber", "Values of transmit F-number must be nonnegative!"},
     {FNUM_ERR_RX_F_NUMBER, "InvalidRXFNumber", "Values of receive F-number must be nonnegative!"},
+    {FNUM_ERR_NOALLOC_TOO_LARGE, "NoAllocScratchTooSmall",
+     "Problem exceeds the 64 MiB static scratch of fnum_das_pw_noalloc!"},
 };
 
 const StatusInfo* find_status(int s) {

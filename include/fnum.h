@@ -58,7 +58,8 @@ typedef enum fnum_status {
   FNUM_ERR_OUT_OF_MEMORY = 20,     /* gpu_bf_error_handling:CUDAError (allocation) */
   FNUM_ERR_INTERNAL = 21,          /* device-side consistency check failed */
   FNUM_ERR_TX_F_NUMBER = 22,       /* gpu_bf_saft_rf:InvalidTXFNumber */
-  FNUM_ERR_RX_F_NUMBER = 23        /* gpu_bf_saft_rf:InvalidRXFNumber */
+  FNUM_ERR_RX_F_NUMBER = 23,       /* gpu_bf_saft_rf:InvalidRXFNumber */
+  FNUM_ERR_NOALLOC_TOO_LARGE = 24  /* fnum_das_pw_noalloc: problem exceeds FNUM_NOALLOC_SCRATCH_BYTES */
 } fnum_status;
 
 /* window ids follow the MEX mapping (+cuda/gpu_bf_helper_functions.cu:56-97) */
@@ -201,6 +202,32 @@ int fnum_plan_execute_dft(fnum_plan* plan, const void* d_rf, int rf_is_double, v
 int fnum_plan_execute_beamform(fnum_plan* plan, void* d_image, float* d_weights, float* d_weights_rx,
                                void* stream);
 int fnum_plan_info_get(const fnum_plan* plan, fnum_plan_info* info);
+
+/* --- plane wave without device allocation ------------------------------- */
+/* No counterpart in the reference (whose gateways allocate and free device
+   memory on every call).  For callers that may not call cudaMalloc -- a
+   real-time acquisition loop that must not block on the allocator, a host
+   that owns a fixed device memory pool, a plug-in inside a process whose
+   device memory belongs to someone else.  It runs the same band DFT and fused
+   beamformer as fnum_plan_execute, but every piece of working memory (tables,
+   twiddles, band spectra, counters, aperture segments) lives in one static
+   device array of FNUM_NOALLOC_SCRATCH_BYTES that the library holds on every
+   GPU that loads it, until the process exits.  Nothing is allocated on the
+   device (host-side tables are built in ordinary host memory).
+     d_rf      device float RF, [n_angles][n_elements][n_samples]
+     d_image   device float2 image [n_out][n_x][n_z] (n_out = 1 with FNUM_FLAG_COMPOUND,
+               else n_angles), scaled by 2 / N_dft; d_weights [n_x][n_z] or NULL
+     flags     0 or FNUM_FLAG_COMPOUND
+   The first call on a device looks up the array's device address (once per
+   device, with that device current): make that first call before any stream
+   capture.  Problems whose tables, spectra and one block of aperture segments
+   do not fit return FNUM_ERR_NOALLOC_TOO_LARGE; larger ones run with as many
+   resident blocks as fit.  All calls share the array and it keeps the last
+   call's contents; everything that must start at zero is cleared per call.
+   Calls whose GPU work overlaps (other streams, other threads) race on it. */
+#define FNUM_NOALLOC_SCRATCH_BYTES (64ull << 20)
+int fnum_das_pw_noalloc(const fnum_pw_desc* desc, const double* steering_angles, int n_angles,
+                        const float* d_rf, int flags, void* d_image, float* d_weights, void* stream);
 /* copies the plan's F table (n_bins values; two tables for SA: tx then rx) */
 int fnum_plan_f_numbers(const fnum_plan* plan, double* values);
 int fnum_plan_destroy(fnum_plan* plan);
