@@ -579,7 +579,7 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
   D.window_id = d->window.id; D.window_par = (float)d->window.parameter;
   D.norm = d->normalization != FNUM_NORMALIZATION_OFF;
   const bool mono = f_monotone(P->F);
-  D.seg_cap = mono ? std::min(b.K, 2 * ne + 16) : b.K;
+  D.seg_cap = (mono ? std::min(b.K, 2 * ne + 16) : b.K) + 1;  // + the sentinel entry
   D.flush_chunks = 4;
   D.scale = (float)(2.0 / b.N);
   D.x_na = na;

@@ -25,6 +25,9 @@
 // bound the phase drift of the recurrence.  u_e is formed in double-float
 // arithmetic and every exponential e^{j 2 pi k u} is reduced exactly to
 // [-1/2, 1/2] cycles before sincospif, so FP32 only carries the final phasor.
+// The plane-wave pre-pass sums each aperture's window in closed form (the
+// elements are equally spaced), and the spectrum chunks are double-buffered
+// in shared memory with cp.async so the next chunk loads during the current one.
 #include "fnum_internal.h"
 
 #include <float.h>
@@ -309,17 +312,67 @@ __device__ __forceinline__ float win_fast(int id, float par, float inv_par, floa
   }
 }
 
-// sum of the apodization over the aperture (the normaliser of one bin)
-__device__ float aperture_sum_fast(const PWDev& d, float inv_par, dfl xm, int emid, int ilb, int iub, float invLl,
-                                   float invLr) {
-  float W = 0.0f;
-  for (int e = ilb; e < emid; ++e) {
-    const dfl c = d.el_m[e];
-    W += win_fast(d.window_id, d.window_par, inv_par, ((xm.x - c.x) + (xm.y - c.y)) * invLl);
+// win_fast with the window id fixed at compile time (the recurrence kernels
+// are instantiated per window, so the boundary handler carries no switch)
+template <int WIN>
+__device__ __forceinline__ float win_t(float par, float inv_par, float u) {
+  if (WIN == 0) return 1.0f;
+  if (WIN == 1) return 0.5f + 0.5f * __cosf(3.14159265358979f * u);
+  if (WIN == 2) {
+    const float thr = 1.0f - par;
+    return (u <= thr) ? 1.0f : 0.5f + 0.5f * __cosf(3.14159265358979f * (u - thr) * inv_par);
   }
-  for (int e = emid; e <= iub; ++e) {
-    const dfl c = d.el_m[e];
-    W += win_fast(d.window_id, d.window_par, inv_par, ((c.x - xm.x) + (c.y - xm.y)) * invLr);
+  if (WIN == 4) return 1.0f - u;
+  return 0.0f;
+}
+
+// Sum of window values over n equally spaced elements at distances
+// l_j = l0 + j p (j < n) from the voxel, all inside the half-width 1/invL:
+//   boxcar      n
+//   triangular  n - (n l0 + p n (n-1) / 2) invL
+//   Hann        n/2 + 1/2 sum_j cos(theta0 + j delta)
+//   Tukey       flat part (u <= 1 - par) counted, the taper summed like Hann
+// with sum_{j<m} cos(t0 + j d) = sin(m d / 2) / sin(d / 2) cos(t0 + (m-1) d / 2).
+__device__ __forceinline__ float cos_series(float t0, float dl, int m) {
+  // angles in units of pi (sinpif / cospif need no large-argument reduction)
+  if (m <= 0) return 0.0f;
+  const float h = 0.5f * dl;
+  const float sh = sinpif(h);
+  const float c = cospif(t0 + (float)(m - 1) * h);
+  return (fabsf(sh) > 1e-6f) ? sinpif((float)m * h) / sh * c : (float)m * c;
+}
+template <int WIN>
+__device__ __forceinline__ float win_sum(float l0, float p, int n, float invL, float par, float inv_par) {
+  if (n <= 0) return 0.0f;
+  const float fn = (float)n;
+  if (WIN == 0) return fn;
+  if (WIN == 4) return fn - (fn * l0 + p * 0.5f * fn * (fn - 1.0f)) * invL;
+  if (WIN == 1) return 0.5f * fn + 0.5f * cos_series(l0 * invL, p * invL, n);
+  if (WIN == 2) {
+    const float thr = 1.0f - par;
+    // elements with u = l invL <= thr form the flat top
+    int n1 = (int)floorf((thr / invL - l0) / p) + 1;
+    n1 = min(max(n1, 0), n);
+    const float t0 = ((l0 + (float)n1 * p) * invL - thr) * inv_par;
+    return (float)n1 + 0.5f * (float)(n - n1) + 0.5f * cos_series(t0, p * invL * inv_par, n - n1);
+  }
+  return 0.0f;
+}
+
+// aperture sum of one bin in closed form: left elements ilb .. emid-1 lie at
+// x - c_e = l0 + j pitch (j counted from emid-1 outwards), right elements
+// emid .. iub at c_e - x = l0 + j pitch (j counted from emid)
+template <int WIN>
+__device__ float aperture_sum_closed(const PWDev& d, float inv_par, dfl xm, int emid, int ilb, int iub,
+                                     float invLl, float invLr) {
+  float W = 0.0f;
+  if (ilb < emid && invLl > 0.0f) {
+    const dfl c = d.el_m[emid - 1];
+    W += win_sum<WIN>((xm.x - c.x) + (xm.y - c.y), d.pitch_f, emid - ilb, invLl, d.window_par, inv_par);
+  }
+  if (iub >= emid && invLr > 0.0f) {
+    const dfl c = d.el_m[emid];
+    W += win_sum<WIN>((c.x - xm.x) + (c.y - xm.y), d.pitch_f, iub - emid + 1, invLr, d.window_par, inv_par);
   }
   return W;
 }
@@ -329,11 +382,15 @@ __device__ float aperture_sum_fast(const PWDev& d, float inv_par, dfl xm, int em
 //   {k_start, i_lb | (i_ub+1) << 16, 1/W, (1/W of the previous segment) / (1/W)}.
 // Also registers, per element, the highest bin at which it is active anywhere
 // in the block (ktop) and the block's element range.
+template <int WIN>
 __device__ int pw_build_segments(const PWDev& d, float inv_par, int ic, int jc, bool valid, int4* seg, int* ktop,
                                  int* e_range, float& W_top, unsigned long long& n_active,
                                  unsigned long long& n_empty) {
   W_top = 0.0f;
-  if (!valid) return 0;
+  if (!valid) {
+    seg[0] = make_int4(-1, seg_code(d.ne, -1), 0, 0);
+    return 0;
+  }
   const dfl xp = d.col_p[ic], zp = d.row_p[jc], xm = d.col_m[ic];
   const int emid = d.col_emid[ic];
   int nseg = 0, prev = -1, u_lo = d.ne, u_hi = -1, act = 0;
@@ -345,10 +402,10 @@ __device__ int pw_build_segments(const PWDev& d, float inv_par, int ic, int jc, 
     if (code != prev) {
       const float Ll = half_left(d.el_lb, xm, ilb, d.ne), Lr = half_right(d.el_ub, xm, iub);
       const float invLl = (Ll > 0.0f) ? 1.0f / Ll : 0.0f, invLr = (Lr > 0.0f) ? 1.0f / Lr : 0.0f;
-      const float W = aperture_sum_fast(d, inv_par, xm, emid, ilb, iub, invLl, invLr);
+      const float W = aperture_sum_closed<WIN>(d, inv_par, xm, emid, ilb, iub, invLl, invLr);
       const float invW = (W > 0.0f) ? (d.norm ? 1.0f / W : 1.0f) : 0.0f;
       const float wr = (invW > 0.0f) ? invW_prev / invW : 0.0f;
-      if (nseg < d.seg_cap)
+      if (nseg < d.seg_cap - 1)
         seg[nseg] = make_int4(kk + d.k_lb, code, __float_as_int(invW), __float_as_int(wr));
       else
         atomicOr(&d.counters[2], ERR_SEG_OVERFLOW);
@@ -371,7 +428,11 @@ __device__ int pw_build_segments(const PWDev& d, float inv_par, int ic, int jc, 
     atomicMin(&e_range[0], u_lo);
     atomicMax(&e_range[1], u_hi);
   }
-  return min(nseg, d.seg_cap);
+  // a sentinel after the last entry lets the recurrence prefetch entries
+  // without testing the list length (its bin, -1, is never reached)
+  nseg = min(nseg, d.seg_cap - 1);
+  seg[nseg] = make_int4(-1, seg_code(d.ne, -1), 0, 0);
+  return nseg;
 }
 
 // last segment whose k_start >= kt (entries sorted by k_start, descending)
@@ -403,16 +464,44 @@ __device__ __forceinline__ float inv_half_width(const dfl* lb_s, const dfl* ub_s
   return __fdividef(1.0f, L);
 }
 
+// asynchronous 8-byte global -> shared copy (completes at cp_async_wait_all)
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Issues the copy of one spectrum chunk (bins kc_lo .. kc_lo + nk - 1 of
+// elements e0 .. e0 + EPT - 1, angles a0 .. a0 + NA - 1) into a shared buffer
+// laid out [bin][element][angle] with rows of ROW float2.
+template <int EPT, int NA>
+__device__ __forceinline__ void pw_stage_chunk(float2* dst, const PWDev& d, int e0, int a0, int kc_lo, int nk,
+                                               int tid) {
+  constexpr int CH = EPT * NA;
+  constexpr int ROW = (CH + 1) & ~1;
+  for (int t = tid; t < nk * CH; t += NTHREADS) {
+    const int kk = t / CH, r = t - kk * CH, q = r / NA, a = r - q * NA;
+    const int e = e0 + q, aa = a0 + a;
+    float2* dp = &dst[kk * ROW + r];
+    if (e < d.ne && aa < d.na)
+      cp_async8(dp, &d.X[((size_t)e * d.K + (kc_lo - d.k_lb + kk)) * d.x_na + d.x_a0 + aa]);
+    else
+      *dp = make_float2(0.0f, 0.0f);
+  }
+  cp_async_commit();
+}
+
 constexpr int SEG_RING = 2;  // segment entries prefetched ahead of the recurrence
 
-template <int EPT, int NA>
+template <int EPT, int NA, int WIN>
 __global__ void __launch_bounds__(NTHREADS, 4)
 pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weights, int n_tiles_x,
                 int n_tiles_z) {
   constexpr int CH = EPT * NA;
   constexpr int ROW = (CH + 1) & ~1;
-  __shared__ __align__(16) float2 xs[KCHUNK * ROW];
-  __shared__ dfl utx_s[NA][NTHREADS];
+  __shared__ __align__(16) float2 xs[2][KCHUNK * ROW];   // double-buffered spectrum chunks
+  __shared__ dfl utx_s[NA][NTHREADS];     // transmit phase per angle, cycles per bin
   __shared__ int e_range[2];
   __shared__ int s_tile;
   extern __shared__ __align__(16) unsigned char dyn[];  // lb[ne], ub[ne] (dfl), ktop[ne]
@@ -448,7 +537,7 @@ pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
     const int ic = min(i, d.nx - 1), jc = min(j, d.nz - 1);
 
     float W_top;
-    const int nseg = pw_build_segments(d, inv_par, ic, jc, valid, seg, ktop, e_range, W_top, n_active, n_empty);
+    const int nseg = pw_build_segments<WIN>(d, inv_par, ic, jc, valid, seg, ktop, e_range, W_top, n_active, n_empty);
     __syncthreads();
     const int E_lo = e_range[0], E_hi = e_range[1];
 
@@ -504,34 +593,33 @@ pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
             const int e = e0 + q;
             const bool left = e < emid;
             const bool act = (e >= lo) && (e <= hi) && (e <= E_hi);
-            aw[q] = act ? win_fast(d.window_id, d.window_par, inv_par,
-                                   dxa[q] * inv_half_width(lb_s, ub_s, xm, left, ilb, iub))
+            aw[q] = act ? win_t<WIN>(d.window_par, inv_par,
+                                     dxa[q] * inv_half_width(lb_s, ub_s, xm, left, ilb, iub))
                         : 0.0f;
             b[q] = aw[q] * invW;
           }
 #pragma unroll
-          for (int r = 0; r < SEG_RING; ++r)
-            if (s + 1 + r < nseg) ring[r] = seg[s + 1 + r];
+          for (int r = 0; r < SEG_RING; ++r) ring[r] = seg[min(s + 1 + r, nseg)];
         } else {
 #pragma unroll
           for (int q = 0; q < EPT; ++q) aw[q] = b[q] = 0.0f;
         }
         float2 part = make_float2(0.0f, 0.0f);
 
-        int kc_hi = kt;
-        while (kc_hi >= d.k_lb) {
-          const int chunk = (kc_hi - d.k_lb) / KCHUNK;
+        // Chunks run from the one holding kt down to chunk 0.  The copy of the
+        // next chunk is in flight while the current one is consumed.
+        const int c_top = (kt - d.k_lb) / KCHUNK;
+        __syncthreads();  // every thread is done with both buffers of the previous pass
+        pw_stage_chunk<EPT, NA>(xs[0], d, e0, a0, d.k_lb + c_top * KCHUNK, kt - (d.k_lb + c_top * KCHUNK) + 1, tid);
+        int buf = 0;
+        for (int chunk = c_top; chunk >= 0; --chunk) {
           const int kc_lo = d.k_lb + chunk * KCHUNK;
-          const int nk = kc_hi - kc_lo + 1;
-          __syncthreads();
-          for (int t = tid; t < nk * CH; t += NTHREADS) {
-            const int kk = t / CH, r = t - kk * CH, q = r / NA, a = r - q * NA;
-            const int e = e0 + q, aa = a0 + a;
-            float2 v = make_float2(0.0f, 0.0f);
-            if (e < d.ne && aa < d.na) v = d.X[((size_t)e * d.K + (kc_lo - d.k_lb + kk)) * d.x_na + d.x_a0 + aa];
-            xs[kk * ROW + r] = v;
-          }
-          __syncthreads();
+          const int kc_hi = (chunk == c_top) ? kt : kc_lo + KCHUNK - 1;
+          cp_async_wait_all();
+          __syncthreads();  // the chunk is visible; the other buffer is free
+          if (chunk > 0) pw_stage_chunk<EPT, NA>(xs[buf ^ 1], d, e0, a0, kc_lo - KCHUNK, KCHUNK, tid);
+          const float2* xb = xs[buf];
+          buf ^= 1;
           for (int k = kc_hi; k >= kc_lo; --k) {
             if (k == ring[0].x) {
               // enter the next segment at bin k
@@ -541,7 +629,7 @@ pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
 #pragma unroll
               for (int r = 0; r + 1 < SEG_RING; ++r) ring[r] = ring[r + 1];
               ++s;
-              ring[SEG_RING - 1] = (s + SEG_RING < nseg) ? seg[s + SEG_RING] : make_int4(-1, 0, 0, 0);
+              ring[SEG_RING - 1] = seg[min(s + SEG_RING, nseg)];
               const int ilb = code_ilb(code), iub = code_iub(code);
               const int lo = min(ilb, emid), hi = max(iub, emid - 1);
 #pragma unroll
@@ -553,7 +641,7 @@ pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
                 float r = wr;
                 if (act) {
                   if ((left ? (ilb != pilb) : (iub != piub)) || bo == 0.0f) {
-                    const float an = win_fast(d.window_id, d.window_par, inv_par,
+                    const float an = win_t<WIN>(d.window_par, inv_par,
                                               dxa[q] * inv_half_width(lb_s, ub_s, xm, left, ilb, iub));
                     r = __fdividef(aw[q], an) * wr;
                     aw[q] = an;
@@ -583,7 +671,7 @@ pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
                 b[q] = bn;
               }
             }
-            const float2* xr = &xs[(k - kc_lo) * ROW];
+            const float2* xr = &xb[(k - kc_lo) * ROW];
 #pragma unroll
             for (int q = 0; q < EPT; ++q) {
 #pragma unroll
@@ -610,7 +698,6 @@ pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
               for (int a = 0; a < NA; ++a) A[q][a] = make_float2(0.0f, 0.0f);
             }
           }
-          kc_hi = kc_lo - 1;
         }
         // compensated accumulation of this element group's contribution
         {
@@ -640,15 +727,25 @@ pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
 
 typedef void (*pw_kernel_t)(const PWDev, float2*, float*, int, int);
 
-static pw_kernel_t pw_pick(int na) {
-  if (na >= 11) return pw_fused_kernel<1, 11>;
-  if (na >= 4) return pw_fused_kernel<2, 4>;
-  if (na >= 2) return pw_fused_kernel<2, 2>;
-  return pw_fused_kernel<4, 1>;
+template <int EPT, int NA>
+static pw_kernel_t pw_pick_win(int window_id) {
+  switch (window_id) {
+    case 0: return pw_fused_kernel<EPT, NA, 0>;
+    case 1: return pw_fused_kernel<EPT, NA, 1>;
+    case 2: return pw_fused_kernel<EPT, NA, 2>;
+    default: return pw_fused_kernel<EPT, NA, 4>;
+  }
+}
+
+static pw_kernel_t pw_pick(int na, int window_id) {
+  if (na >= 11) return pw_pick_win<1, 11>(window_id);
+  if (na >= 4) return pw_pick_win<2, 4>(window_id);
+  if (na >= 2) return pw_pick_win<2, 2>(window_id);
+  return pw_pick_win<4, 1>(window_id);
 }
 
 int pw_fused_grid(const PWDev& d, int* blocks_per_sm) {
-  pw_kernel_t fn = pw_pick(d.na);
+  pw_kernel_t fn = pw_pick(d.na, d.window_id);
   int dev = 0, nsm = 0, bps = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -665,7 +762,7 @@ cudaError_t launch_pw_fused(const PWDev& d, int grid, float2* image, float* weig
   // each launch draws tiles from a fresh counter
   cudaError_t e = cudaMemsetAsync(d.counters + 3, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
-  pw_pick(d.na)<<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, ntz);
+  pw_pick(d.na, d.window_id)<<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, ntz);
   return cudaGetLastError();
 }
 // ---------------------------------------------------------------------------

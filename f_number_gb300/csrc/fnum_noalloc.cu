@@ -185,9 +185,10 @@ extern "C" int fnum_das_pw_noalloc(const fnum_pw_desc* desc, const double* steer
   D.nx = nx; D.nz = nz; D.ne = ne; D.na = na; D.K = K; D.k_lb = k_lb; D.k_ub = k_ub; D.N_dft = N;
   D.window_id = wid; D.window_par = (float)desc->window.parameter;
   D.norm = desc->normalization != FNUM_NORMALIZATION_OFF;
-  D.seg_cap = mono ? (K < 2 * ne + 16 ? K : 2 * ne + 16) : K;
+  D.seg_cap = (mono ? (K < 2 * ne + 16 ? K : 2 * ne + 16) : K) + 1;  // + the sentinel entry
   D.flush_chunks = 4;
   D.scale = (float)(2.0 / N);
+  D.pitch_f = (float)pitch;  // element spacing of the closed-form aperture sums
   D.x_na = na;
   D.x_a0 = 0;
   unsigned long long* counters = cv.take<unsigned long long>(8);
