@@ -43,6 +43,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--grid", type=int, default=512, help="voxels per side (512 = the benchmark grid; smaller "
                     "sizes keep the same 0.06 mm spacing, for profiling)")
+    ap.add_argument("--workload", default="cpwc", choices=["cpwc", "saft"],
+                    help="cpwc (default, the headline) or saft: 128 x 128 synthetic aperture, 3072 samples at "
+                    "40 MHz, 400 x 400 voxels, directivity F-number, boxcar windows")
+    ap.add_argument("--band", default="full", choices=["full", "2-7"],
+                    help="saft band: the gateway default [DBL_MIN, f_s/2] or 2-7 MHz")
     return ap.parse_args()
 
 
@@ -252,11 +257,24 @@ def run_ours(args):
     peak = _lib.C.c_double(0.0)
     _lib.check(_lib.lib().fnum_diag_fp32_peak(local, _lib.C.byref(peak)))
     bf_avg_ms = float(np.mean(bf_ms))
+    if args.kernel == "plain":
+        # the plain kernel keeps no counters; the active-term count is a property of
+        # the workload, taken from one untimed run of the fused kernel on the same plan
+        fplan = das.PWPlan(wl.positions_x, wl.positions_z, wl.n_samples, wl.array.n_elements, wl.f_s, wl.angles,
+                           wl.array.width, wl.array.pitch, wl.c, list(wl.f_bounds), 0.0, win, fn, device=local,
+                           compound=True, kernel="fused")
+        fplan.execute_dft(rf, stream)
+        fplan.execute_beamform(img, wts, stream=stream)
+        torch.cuda.synchronize()
+        finfo = fplan.info()
+        fplan.close()
+        info = dict(info, active_terms=finfo["active_terms"], executed_terms=info["terms"])
     flops = 8.0 * info["active_terms"]
     achieved = flops / (bf_avg_ms * 1e-3) / 1e12
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
             "frac": achieved / peak.value if peak.value else None, "traffic": traffic_from_profiles(),
-            "kernel": "pw_fused_kernel<1,11>", "work": "8 FLOP per active voxel x element x bin x angle term "
+            "kernel": "pw_plain_kernel" if args.kernel == "plain" else "pw_fused_kernel<1,11,hann>",
+            "work": "8 FLOP per active voxel x element x bin x angle term "
             "(complex MAC); %d active of %d nominal terms" % (info["active_terms"], info["terms"]),
             "executed_terms": info["executed_terms"],
             "peak_source": "measured FP32 FMA throughput (fnum_diag_fp32_peak); MEASURED_PEAKS.json "
@@ -280,11 +298,92 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# synthetic-aperture workload (reported beside the headline; same contract)
+# ---------------------------------------------------------------------------
+SA_METRIC = "SAFT frames/s (128 tx x 128 rx, 3072 smp, 400x400)"
+
+
+def saft_workload(band):
+    from f_number_gb300 import synth
+    return synth.saft_128(seed=0, f_bounds=None if band == "full" else (2e6, 7e6))
+
+
+def saft_config(wl, kernel, band):
+    return {"workload": "saft_128x128_3072smp_40MHz_400x400_%s_boxcar_perrot" % ("fullband" if band == "full"
+                                                                                   else "2-7MHz"),
+            "n_elements": wl.array.n_elements, "n_samples": wl.n_samples, "grid": [400, 400], "kernel": kernel,
+            "l2": "inputs larger than L2 (201 MB RF, band spectra up to 261 MB)", "data": "synthetic seeded RF"}
+
+
+def run_saft(args):
+    import torch
+    from f_number_gb300 import _lib, das, f_numbers, windows
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    wl = saft_workload(args.band)
+    fn = f_numbers.directivity.perrot(0.918)
+    plan = das.SAPlan(wl.positions_x, wl.positions_z, wl.n_samples, wl.array.n_elements, wl.f_s, wl.array.width,
+                      wl.array.pitch, wl.c, wl.f_bounds, 0.0, windows.boxcar(), windows.boxcar(), fn, fn,
+                      device=local, kernel=args.kernel)
+    rf = torch.tensor(wl.rf, dtype=torch.float32, device=dev)                 # [tx, rx, t]
+    img = torch.empty((1, plan.n_x, plan.n_z), dtype=torch.complex64, device=dev)
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        plan.execute_dft(rf, stream)
+        plan.execute_beamform(img, stream=stream)
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    for s in range(args.steps):
+        e0, e1, e2 = evs[s]
+        e0.record(stream)
+        plan.execute_dft(rf, stream)
+        e1.record(stream)
+        plan.execute_beamform(img, stream=stream)
+        e2.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(c) for a, b, c in evs]
+    bf_ms = float(np.mean([b.elapsed_time(c) for a, b, c in evs]))
+    info = plan.info()
+    value = args.steps / (sum(step_ms) * 1e-3)
+    peak = _lib.C.c_double(0.0)
+    _lib.check(_lib.lib().fnum_diag_fp32_peak(local, _lib.C.byref(peak)))
+    active = info["active_terms"] if args.kernel == "fused" else info["terms"]
+    achieved = 8.0 * active / (bf_ms * 1e-3) / 1e12
+    roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+            "frac": achieved / peak.value if peak.value else None, "traffic": None,
+            "kernel": "sa_fused_kernel<8>" if args.kernel == "fused" else "sa_plain_kernel",
+            "work": "8 FLOP per active voxel x tx x rx x bin term; %d active of %d nominal terms"
+            % (info["active_terms"], info["terms"]),
+            "peak_source": "measured FP32 FMA throughput (fnum_diag_fp32_peak)"}
+    if rank != 0:
+        return
+    out = {"metric": SA_METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": float(np.mean(step_ms)), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32 (double-float phase)", "data": "synthetic",
+           "config": saft_config(wl, args.kernel, args.band),
+           "gterms_per_s": info["terms"] / (np.mean(step_ms) * 1e-3) / 1e9,
+           "stage_ms": {"band_dft": float(np.mean([a.elapsed_time(b) for a, b, c in evs])), "beamform": bf_ms},
+           "roofline": roof, "clocks": clk, "gpu_launches": 2 * args.steps}
+    print(json.dumps(out))
+    plan.close()
+
+
 def main():
     args = parse()
     import __graft_entry__ as g
     g.build()
-    if args.impl == "reference":
+    if args.workload == "saft":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the saft workload has no CPU arm; the CPU "
+                              "baseline of the headline is the cpwc workload"}))
+            return
+        run_saft(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
