@@ -700,7 +700,7 @@ int make_sa_plan(const fnum_sa_desc* d, int flags, fnum_plan** out) {
   D.norm_rx = on_rx;
   D.last_bin_only = last_bin_only;
   const bool mono = f_monotone(Ftx) && f_monotone(Frx);
-  D.seg_cap = mono ? std::min(bk.K, 4 * ne + 32) : bk.K;
+  D.seg_cap = (mono ? std::min(bk.K, 4 * ne + 32) : bk.K) + 1;  // + the sentinel entry
   D.flush_chunks = 4;
   D.scale = (float)(2.0 / b.N);
   std::vector<dfl> gt, gr;

@@ -20,10 +20,11 @@ constexpr int KCHUNK = 64;
 // one aperture segment of one voxel (bins k_start down to the next entry's
 // k_start + 1 share the same apertures).  Plane wave: one int4
 // {k_start, i_lb | (i_ub+1) << 16, 1/W, ratio of 1/W to the previous segment};
-// SAFT: two int4 {k_start, code, 1/W, W}, tx then rx.  Kernels and the host's
-// scratch allocation both size entries with these constants.
+// SAFT: one int4 {k_start, tx code, rx code, 1/(W_tx W_rx)}.  Each list ends
+// with a sentinel entry.  Kernels and the host's scratch allocation both size
+// entries with these constants.
 constexpr int PW_SEG_INT4 = 1;
-constexpr int SA_SEG_INT4 = 2;
+constexpr int SA_SEG_INT4 = 1;
 
 struct PWDev {
   int nx, nz, ne, na, K, k_lb, k_ub, N_dft;
@@ -78,7 +79,7 @@ struct SADev {
   const dfl* el_u; const dfl* el_m; const dfl* el_lb; const dfl* el_ub;
   const dfl* gtx; const dfl* grx;   // [K]
   float2* X;                        // [ntx][nrx][K]
-  int4* seg;                        // [grid][NTHREADS][seg_cap][2]
+  int4* seg;                        // [grid][NTHREADS][seg_cap]
   unsigned long long* counters;
   const float* px_f; const float* pz_f; const float* ctr_f; const float* lb_f; const float* ub_f;
   const float* Ftx_f; const float* Frx_f;

@@ -848,14 +848,52 @@ cudaError_t launch_pw_plain(const PWDev& d, float2* image, float* weights, cudaS
 // ---------------------------------------------------------------------------
 // fused synthetic-aperture kernel
 // ---------------------------------------------------------------------------
-// Segments carry both apertures: seg[2s] = {k_start, tx code, invWtx, Wtx},
-// seg[2s+1] = {k_start, rx code, invWrx, Wrx}.  The weight of pair (t, r) is
-// a_tx(t) a_rx(r) / (Wtx Wrx) with the normalisations that are on.
+// One segment entry per aperture change of a voxel (bins k_start down to the
+// next entry's k_start + 1 share both apertures):
+//   {k_start, tx code, rx code, 1/(W_tx W_rx)}
+// with the sums of the normalisations that are on (1 for one that is off, 0
+// for an empty aperture).  A sentinel entry (k_start = -1) ends every list.
+// The weight of the pair (t, r) is a_tx(t) a_rx(r) / (W_tx W_rx).
+
+// window sum of one aperture in closed form, window id known at run time
+__device__ __forceinline__ float win_sum_rt(int id, float l0, float p, int n, float invL, float par, float inv_par) {
+  switch (id) {
+    case 0: return win_sum<0>(l0, p, n, invL, par, inv_par);
+    case 1: return win_sum<1>(l0, p, n, invL, par, inv_par);
+    case 2: return win_sum<2>(l0, p, n, invL, par, inv_par);
+    case 4: return win_sum<4>(l0, p, n, invL, par, inv_par);
+    default: return 0.0f;
+  }
+}
+__device__ float sa_aperture_sum(const SADev& d, int id, float par, dfl xm, int emid, int ilb, int iub) {
+  const float inv_par = (par > 0.0f) ? 1.0f / par : 0.0f;
+  float W = 0.0f;
+  if (ilb < emid) {
+    const float L = half_left(d.el_lb, xm, ilb, d.ne);
+    if (L > 0.0f) {
+      const dfl c = d.el_m[emid - 1];
+      W += win_sum_rt(id, (xm.x - c.x) + (xm.y - c.y), d.pitch_f, emid - ilb, 1.0f / L, par, inv_par);
+    }
+  }
+  if (iub >= emid) {
+    const float L = half_right(d.el_ub, xm, iub);
+    if (L > 0.0f) {
+      const dfl c = d.el_m[emid];
+      W += win_sum_rt(id, (c.x - xm.x) + (c.y - xm.y), d.pitch_f, iub - emid + 1, 1.0f / L, par, inv_par);
+    }
+  }
+  return W;
+}
+
 __device__ int sa_build_segments(const SADev& d, int ic, int jc, bool valid, int4* seg, int* ktop_tx, int* ktop_rx,
                                  int* ranges, float& Wtx_top, float& Wrx_top, unsigned long long& n_active,
                                  unsigned long long& n_empty) {
+  const int4 sentinel = make_int4(-1, seg_code(d.ne, -1), seg_code(d.ne, -1), 0);
   Wtx_top = Wrx_top = 0.0f;
-  if (!valid) return 0;
+  if (!valid) {
+    seg[0] = sentinel;
+    return 0;
+  }
   const dfl xp = d.col_p[ic], zp = d.row_p[jc], xm = d.col_m[ic];
   const int emid = d.col_emid[ic];
   int nseg = 0, prev_t = -1, prev_r = -1;
@@ -867,16 +905,14 @@ __device__ int sa_build_segments(const SADev& d, int ic, int jc, bool valid, int
     aperture(xp, zp, d.grx[kk], d.ne, rlb, rub);
     const int ct = seg_code(tlb, tub), cr = seg_code(rlb, rub);
     if (ct != prev_t || cr != prev_r) {
-      const float Wt = aperture_sum(d.wtx_id, d.wtx_par, d.el_m, d.el_lb, d.el_ub, xm, d.ne, emid, tlb, tub);
-      const float Wr = aperture_sum(d.wrx_id, d.wrx_par, d.el_m, d.el_lb, d.el_ub, xm, d.ne, emid, rlb, rub);
+      const float Wt = sa_aperture_sum(d, d.wtx_id, d.wtx_par, xm, emid, tlb, tub);
+      const float Wr = sa_aperture_sum(d, d.wrx_id, d.wrx_par, xm, emid, rlb, rub);
       const float it = (Wt > 0.0f) ? (d.norm_tx ? 1.0f / Wt : 1.0f) : 0.0f;
       const float ir = (Wr > 0.0f) ? (d.norm_rx ? 1.0f / Wr : 1.0f) : 0.0f;
-      if (nseg < d.seg_cap) {
-        seg[2 * nseg] = make_int4(kk + d.k_lb, ct, __float_as_int(it), __float_as_int(Wt));
-        seg[2 * nseg + 1] = make_int4(kk + d.k_lb, cr, __float_as_int(ir), __float_as_int(Wr));
-      } else {
+      if (nseg < d.seg_cap - 1)
+        seg[nseg] = make_int4(kk + d.k_lb, ct, cr, __float_as_int(it * ir));
+      else
         atomicOr(&d.counters[2], ERR_SEG_OVERFLOW);
-      }
       if (nseg == 0) {
         Wtx_top = Wt;
         Wrx_top = Wr;
@@ -910,47 +946,103 @@ __device__ int sa_build_segments(const SADev& d, int ic, int jc, bool valid, int
     atomicMin(&ranges[2], r_lo);
     atomicMax(&ranges[3], r_hi);
   }
-  return min(nseg, d.seg_cap);
+  nseg = min(nseg, d.seg_cap - 1);
+  seg[nseg] = sentinel;
+  return nseg;
 }
 
+// last segment whose k_start >= kt (entries sorted by k_start, descending)
 __device__ __forceinline__ int sa_seg_find(const int4* seg, int nseg, int kt) {
   int lo = 0, hi = nseg - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (seg[2 * mid].x >= kt) lo = mid; else hi = mid - 1;
+    if (seg[mid].x >= kt) lo = mid; else hi = mid - 1;
   }
   return lo;
 }
 
+// window value of element e for the aperture (ilb, iub) of a voxel at xm,
+// 0 outside (edges from shared memory)
+template <int WIN>
+__device__ __forceinline__ float sa_apod(const dfl* lb_s, const dfl* ub_s, dfl xm, int e, int emid, int ilb, int iub,
+                                         float dxa, float par, float inv_par) {
+  const bool left = e < emid;
+  if (left ? (e < ilb) : (e > iub)) return 0.0f;
+  return win_t<WIN>(par, inv_par, dxa * inv_half_width(lb_s, ub_s, xm, left, ilb, iub));
+}
+
+// Issues the copy of one spectrum chunk (bins kc_lo .. kc_lo + nk - 1 of the
+// receive elements r0 .. r0 + EPT - 1 of transmit t) into a shared buffer laid
+// out [bin][receive] with rows of ROW float2; consecutive threads copy
+// consecutive bins of one receive element.
 template <int EPT>
-__global__ void __launch_bounds__(NTHREADS)
-sa_fused_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ wtx_out, float* __restrict__ wrx_out,
-                int n_tiles_x, int n_tiles, int weights_only) {
+__device__ __forceinline__ void sa_stage_chunk(float2* dst, const SADev& d, int t, int r0, int kc_lo, int nk, int tid) {
   constexpr int ROW = (EPT + 1) & ~1;
-  __shared__ __align__(16) float2 xs[KCHUNK * ROW];
+  for (int idx = tid; idx < KCHUNK * EPT; idx += NTHREADS) {
+    const int kk = idx % KCHUNK, q = idx / KCHUNK;
+    const int r = r0 + q;
+    if (kk < nk && r < d.ne) cp_async8(&dst[kk * ROW + q], &d.X[((size_t)t * d.ne + r) * d.K + (kc_lo - d.k_lb + kk)]);
+    else if (kk < nk) dst[kk * ROW + q] = make_float2(0.0f, 0.0f);
+  }
+  cp_async_commit();
+}
+
+template <int EPT, int WT, int WR>
+__global__ void __launch_bounds__(NTHREADS, 4)
+sa_fused_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ wtx_out, float* __restrict__ wrx_out,
+                int n_tiles_x, int n_tiles_z, int weights_only) {
+  constexpr int ROW = (EPT + 1) & ~1;
+  __shared__ __align__(16) float2 xs[2][KCHUNK * ROW];
   __shared__ int ranges[4];
-  extern __shared__ int ktops[];  // [2][ne]
-  int* ktop_tx = ktops;
-  int* ktop_rx = ktops + d.ne;
+  __shared__ int s_tile;
+  __shared__ unsigned long long s_count[2];         // active terms, zero-weight bins
+  __shared__ float dxq_s[EPT][NTHREADS];            // |c_r - x| of the pass's receive elements
+  extern __shared__ __align__(16) unsigned char dyn[];  // lb[ne], ub[ne] (dfl), ktop_tx[ne], ktop_rx[ne]
+  dfl* lb_s = (dfl*)dyn;
+  dfl* ub_s = lb_s + d.ne;
+  int* ktop_tx = (int*)(ub_s + d.ne);
+  int* ktop_rx = ktop_tx + d.ne;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int n_tiles = n_tiles_x * n_tiles_z;
   int4* seg = d.seg + ((size_t)blockIdx.x * NTHREADS + tid) * (size_t)d.seg_cap * SA_SEG_INT4;
-  unsigned long long n_active = 0, n_empty = 0;
+  const float ipt = (d.wtx_par > 0.0f) ? 1.0f / d.wtx_par : 0.0f;
+  const float ipr = (d.wrx_par > 0.0f) ? 1.0f / d.wrx_par : 0.0f;
+  unsigned long long n_exec = 0;
+  if (tid == 0) s_count[0] = s_count[1] = 0ull;
+  for (int e = tid; e < d.ne; e += NTHREADS) {
+    lb_s[e] = d.el_lb[e];
+    ub_s[e] = d.el_ub[e];
+  }
 
-  for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-    const int i = (tile % n_tiles_x) * TILE_X + warp;
-    const int j = (tile / n_tiles_x) * TILE_Z + lane;
-    const bool valid = (i < d.nx) && (j < d.nz);
-    const int ic = min(i, d.nx - 1), jc = min(j, d.nz - 1);
-    for (int e = tid; e < 2 * d.ne; e += NTHREADS) ktops[e] = -1;
+  for (;;) {
+    if (tid == 0) s_tile = (int)atomicAdd(&d.counters[3], 1ull);
+    for (int e = tid; e < 2 * d.ne; e += NTHREADS) ktop_tx[e] = -1;
     if (tid == 0) {
       ranges[0] = ranges[2] = d.ne;
       ranges[1] = ranges[3] = -1;
     }
     __syncthreads();
-    float Wtx_top, Wrx_top;
-    const int nseg = sa_build_segments(d, ic, jc, valid, seg, ktop_tx, ktop_rx, ranges, Wtx_top, Wrx_top, n_active,
-                                       n_empty);
+    const int tile = s_tile;
+    if (tile >= n_tiles) break;
+    int tx_, tz_;
+    tile_coords(tile, n_tiles_x, n_tiles_z, tx_, tz_);
+    const int i = tx_ * TILE_X + warp;
+    const int j = tz_ * TILE_Z + lane;
+    const bool valid = (i < d.nx) && (j < d.nz);
+    const int ic = min(i, d.nx - 1), jc = min(j, d.nz - 1);
+    int nseg;
+    {
+      float Wtx_top, Wrx_top;
+      unsigned long long n_active = 0, n_empty = 0;
+      nseg = sa_build_segments(d, ic, jc, valid, seg, ktop_tx, ktop_rx, ranges, Wtx_top, Wrx_top, n_active, n_empty);
+      atomicAdd(&s_count[0], n_active);
+      atomicAdd(&s_count[1], n_empty);
+      if (valid) {
+        if (wtx_out) wtx_out[(size_t)ic * d.nz + jc] = Wtx_top;
+        if (wrx_out) wrx_out[(size_t)ic * d.nz + jc] = Wrx_top;
+      }
+    }
     __syncthreads();
     const int T_lo = ranges[0], T_hi = weights_only ? -1 : ranges[1], R_lo = ranges[2], R_hi = ranges[3];
 
@@ -962,7 +1054,7 @@ sa_fused_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
       const int kt_t = ktop_tx[t];
       if (kt_t < d.k_lb) continue;
       const dfl ctm = d.el_m[t];
-      const float dxt = (ctm.x - xm.x) + (ctm.y - xm.y);
+      const float dxt = fabsf((ctm.x - xm.x) + (ctm.y - xm.y));
       const dfl utx = df_sqrt(df_add(df_sqr(df_sub(d.el_u[t], xu)), zu2));
       for (int r0 = R_lo; r0 <= R_hi; r0 += EPT) {
         int kt = -1;
@@ -971,97 +1063,93 @@ sa_fused_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
           if (r0 + q <= R_hi) kt = max(kt, ktop_rx[r0 + q]);
         kt = min(kt, kt_t);
         if (kt < d.k_lb) continue;
-        float dxq[EPT], b[EPT];
-        dfl u[EPT];
+        if (tid == 0) n_exec += (unsigned long long)(kt - d.k_lb + 1) * EPT * NTHREADS;
+        // weight of chain q: f * ar[q], f = a_tx(t) / (W_tx W_rx) shared by the pass
+        float ar[EPT];
         float2 z[EPT], A[EPT];
 #pragma unroll
         for (int q = 0; q < EPT; ++q) {
           const int e = min(r0 + q, d.ne - 1);
           const dfl cm = d.el_m[e];
-          dxq[q] = (cm.x - xm.x) + (cm.y - xm.y);
-          const dfl urx = df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2));
-          u[q] = df_add(urx, utx);
-          z[q] = cis_ku(1, u[q]);
+          dxq_s[q][tid] = fabsf((cm.x - xm.x) + (cm.y - xm.y));
+          z[q] = cis_ku(1, df_add(df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2)), utx));
           A[q] = make_float2(0.0f, 0.0f);
         }
-        int s = 0, nb = -1;
-        int4 ct = make_int4(0, seg_code(d.ne, -1), 0, 0), cr = ct, nt_ = ct, nr_ = ct;
+        // segment in effect at kt and the prefetch ring of the following entries
+        int s = 0;
+        int4 cur = make_int4(-1, seg_code(d.ne, -1), seg_code(d.ne, -1), 0);
+        int4 ring[SEG_RING];
         if (nseg > 0) {
           s = sa_seg_find(seg, nseg, kt);
-          ct = seg[2 * s];
-          cr = seg[2 * s + 1];
-          if (s + 1 < nseg) {
-            nt_ = seg[2 * s + 2];
-            nr_ = seg[2 * s + 3];
-            nb = nt_.x;
-          }
+          cur = seg[s];
         }
-        float atx;
+#pragma unroll
+        for (int r = 0; r < SEG_RING; ++r) ring[r] = seg[min(s + 1 + r, nseg)];
+        float at, f;
         {
-          const int tlb = code_ilb(ct.y), tub = code_iub(ct.y), rlb = code_ilb(cr.y), rub = code_iub(cr.y);
-          atx = elem_apod(d.wtx_id, d.wtx_par, t, emid, tlb, tub, dxt, half_left(d.el_lb, xm, tlb, d.ne),
-                          half_right(d.el_ub, xm, tub)) * __int_as_float(ct.z);
-          const float Ll = half_left(d.el_lb, xm, rlb, d.ne), Lr = half_right(d.el_ub, xm, rub);
-          const float ir = __int_as_float(cr.z);
+          const int tlb = code_ilb(cur.y), tub = code_iub(cur.y), rlb = code_ilb(cur.z), rub = code_iub(cur.z);
+          at = sa_apod<WT>(lb_s, ub_s, xm, t, emid, tlb, tub, dxt, d.wtx_par, ipt);
+          f = at * __int_as_float(cur.w);
 #pragma unroll
           for (int q = 0; q < EPT; ++q) {
             const int e = r0 + q;
-            b[q] = (e <= R_hi) ? atx * elem_apod(d.wrx_id, d.wrx_par, e, emid, rlb, rub, dxq[q], Ll, Lr) * ir : 0.0f;
+            ar[q] = (e <= R_hi) ? sa_apod<WR>(lb_s, ub_s, xm, e, emid, rlb, rub, dxq_s[q][tid], d.wrx_par, ipr)
+                                : 0.0f;
           }
         }
         float2 part = make_float2(0.0f, 0.0f);
-        int kc_hi = kt;
-        while (kc_hi >= d.k_lb) {
-          const int chunk = (kc_hi - d.k_lb) / KCHUNK;
+        const int c_top = (kt - d.k_lb) / KCHUNK;
+        __syncthreads();  // every thread is done with both buffers of the previous pass
+        sa_stage_chunk<EPT>(xs[0], d, t, r0, d.k_lb + c_top * KCHUNK, kt - (d.k_lb + c_top * KCHUNK) + 1, tid);
+        int buf = 0;
+        for (int chunk = c_top; chunk >= 0; --chunk) {
           const int kc_lo = d.k_lb + chunk * KCHUNK;
-          const int nk = kc_hi - kc_lo + 1;
+          const int kc_hi = (chunk == c_top) ? kt : kc_lo + KCHUNK - 1;
+          cp_async_wait_all();
           __syncthreads();
-          for (int x = tid; x < nk * EPT; x += NTHREADS) {
-            const int kk = x / EPT, q = x - kk * EPT;
-            const int e = r0 + q;
-            float2 v = make_float2(0.0f, 0.0f);
-            if (e < d.ne) v = d.X[((size_t)t * d.ne + e) * d.K + (kc_lo - d.k_lb + kk)];
-            xs[kk * ROW + q] = v;
-          }
-          __syncthreads();
+          if (chunk > 0) sa_stage_chunk<EPT>(xs[buf ^ 1], d, t, r0, kc_lo - KCHUNK, KCHUNK, tid);
+          const float2* xb = xs[buf];
+          buf ^= 1;
           for (int k = kc_hi; k >= kc_lo; --k) {
-            if (k == nb) {
+            if (k == ring[0].x) {
+              // enter the next segment at bin k
+              const int ptc = cur.y, prc = cur.z;
+              const float fo = f;
+              cur = ring[0];
+#pragma unroll
+              for (int r = 0; r + 1 < SEG_RING; ++r) ring[r] = ring[r + 1];
               ++s;
-              ct = nt_;
-              cr = nr_;
-              nb = -1;
-              if (s + 1 < nseg) {
-                nt_ = seg[2 * s + 2];
-                nr_ = seg[2 * s + 3];
-                nb = nt_.x;
-              }
-              const int tlb = code_ilb(ct.y), tub = code_iub(ct.y), rlb = code_ilb(cr.y), rub = code_iub(cr.y);
-              const float atn = elem_apod(d.wtx_id, d.wtx_par, t, emid, tlb, tub, dxt, half_left(d.el_lb, xm, tlb, d.ne),
-                                          half_right(d.el_ub, xm, tub)) * __int_as_float(ct.z);
-              const float Ll = half_left(d.el_lb, xm, rlb, d.ne), Lr = half_right(d.el_ub, xm, rub);
-              const float ir = __int_as_float(cr.z);
+              ring[SEG_RING - 1] = seg[min(s + SEG_RING, nseg)];
+              const int tlb = code_ilb(cur.y), tub = code_iub(cur.y), rlb = code_ilb(cur.z), rub = code_iub(cur.z);
+              if (cur.y != ptc || at == 0.0f) at = sa_apod<WT>(lb_s, ub_s, xm, t, emid, tlb, tub, dxt, d.wtx_par, ipt);
+              f = at * __int_as_float(cur.w);
+              const bool rx_changed = cur.z != prc;
+              const float rf = (fo != 0.0f && f != 0.0f) ? __fdividef(fo, f) : 0.0f;
 #pragma unroll
               for (int q = 0; q < EPT; ++q) {
                 const int e = r0 + q;
-                const float bn =
-                    (e <= R_hi) ? atn * elem_apod(d.wrx_id, d.wrx_par, e, emid, rlb, rub, dxq[q], Ll, Lr) * ir : 0.0f;
-                const float bo = b[q];
+                const float ao = ar[q];
+                float an = ao;
+                if (rx_changed || ao == 0.0f)
+                  an = (e <= R_hi) ? sa_apod<WR>(lb_s, ub_s, xm, e, emid, rlb, rub, dxq_s[q][tid], d.wrx_par, ipr) : 0.0f;
+                const float bo = fo * ao, bn = f * an;
                 if (bn != 0.0f && bo != 0.0f) {
-                  const float r = bo / bn;
+                  const float r = (an == ao) ? rf : __fdividef(bo, bn);
                   A[q].x *= r;
                   A[q].y *= r;
                 } else {
-                  if (bo != 0.0f) {
-                    const float2 tt = cmul(cis_ku(k + 1, u[q]), A[q]);
+                  if (bo != 0.0f) {  // leaves the aperture below k+1: flush at k+1
+                    const dfl u = df_add(df_sqrt(df_add(df_sqr(df_sub(d.el_u[min(e, d.ne - 1)], xu)), zu2)), utx);
+                    const float2 tt = cmul(cis_ku(k + 1, u), A[q]);
                     part.x = fmaf(bo, tt.x, part.x);
                     part.y = fmaf(bo, tt.y, part.y);
                   }
                   A[q] = make_float2(0.0f, 0.0f);
                 }
-                b[q] = bn;
+                ar[q] = an;
               }
             }
-            const float2* xr = &xs[(k - kc_lo) * ROW];
+            const float2* xr = &xb[(k - kc_lo) * ROW];
 #pragma unroll
             for (int q = 0; q < EPT; ++q) {
               const float2 x = xr[q];
@@ -1073,15 +1161,16 @@ sa_fused_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
           if (chunk % d.flush_chunks == 0) {
 #pragma unroll
             for (int q = 0; q < EPT; ++q) {
-              if (b[q] != 0.0f) {
-                const float2 tt = cmul(cis_ku(kc_lo, u[q]), A[q]);
-                part.x = fmaf(b[q], tt.x, part.x);
-                part.y = fmaf(b[q], tt.y, part.y);
+              const float bq = f * ar[q];
+              if (bq != 0.0f) {
+                const dfl u = df_add(df_sqrt(df_add(df_sqr(df_sub(d.el_u[min(r0 + q, d.ne - 1)], xu)), zu2)), utx);
+                const float2 tt = cmul(cis_ku(kc_lo, u), A[q]);
+                part.x = fmaf(bq, tt.x, part.x);
+                part.y = fmaf(bq, tt.y, part.y);
               }
               A[q] = make_float2(0.0f, 0.0f);
             }
           }
-          kc_hi = kc_lo - 1;
         }
         float y = part.x - comp.x, tt = acc.x + y;
         comp.x = (tt - acc.x) - y;
@@ -1092,24 +1181,43 @@ sa_fused_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
         acc.y = tt;
       }
     }
-    if (valid) {
-      image[(size_t)ic * d.nz + jc] = make_float2(acc.x * d.scale, acc.y * d.scale);
-      if (wtx_out) wtx_out[(size_t)ic * d.nz + jc] = Wtx_top;
-      if (wrx_out) wrx_out[(size_t)ic * d.nz + jc] = Wrx_top;
-    }
+    if (valid) image[(size_t)ic * d.nz + jc] = make_float2(acc.x * d.scale, acc.y * d.scale);
     __syncthreads();
   }
-  atomicAdd(&d.counters[0], n_active);
-  atomicAdd(&d.counters[1], n_empty);
+  if (tid == 0) {
+    atomicAdd(&d.counters[0], s_count[0]);
+    atomicAdd(&d.counters[1], s_count[1]);
+    atomicAdd(&d.counters[4], n_exec);
+  }
 }
 
 constexpr int SA_EPT = 8;
+typedef void (*sa_kernel_t)(const SADev, float2*, float*, float*, int, int, int);
+
+template <int WT>
+static sa_kernel_t sa_pick_rx(int wr) {
+  switch (wr) {
+    case 0: return sa_fused_kernel<SA_EPT, WT, 0>;
+    case 1: return sa_fused_kernel<SA_EPT, WT, 1>;
+    case 2: return sa_fused_kernel<SA_EPT, WT, 2>;
+    default: return sa_fused_kernel<SA_EPT, WT, 4>;
+  }
+}
+static sa_kernel_t sa_pick(int wt, int wr) {
+  switch (wt) {
+    case 0: return sa_pick_rx<0>(wr);
+    case 1: return sa_pick_rx<1>(wr);
+    case 2: return sa_pick_rx<2>(wr);
+    default: return sa_pick_rx<4>(wr);
+  }
+}
+static size_t sa_smem(const SADev& d) { return (size_t)d.ne * (2 * sizeof(dfl) + 2 * sizeof(int)); }
 
 int sa_fused_grid(const SADev& d, int* blocks_per_sm) {
   int dev = 0, nsm = 0, bps = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, sa_fused_kernel<SA_EPT>, NTHREADS, (size_t)2 * d.ne * sizeof(int));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, sa_pick(d.wtx_id, d.wrx_id), NTHREADS, sa_smem(d));
   if (bps < 1) bps = 1;
   if (blocks_per_sm) *blocks_per_sm = bps;
   const int tiles = ((d.nx + TILE_X - 1) / TILE_X) * ((d.nz + TILE_Z - 1) / TILE_Z);
@@ -1117,10 +1225,12 @@ int sa_fused_grid(const SADev& d, int* blocks_per_sm) {
 }
 
 cudaError_t launch_sa_fused(const SADev& d, int grid, float2* image, float* wtx, float* wrx, cudaStream_t s) {
-  const int ntx = (d.nx + TILE_X - 1) / TILE_X;
-  const int tiles = ntx * ((d.nz + TILE_Z - 1) / TILE_Z);
-  sa_fused_kernel<SA_EPT><<<grid, NTHREADS, (size_t)2 * d.ne * sizeof(int), s>>>(d, image, wtx, wrx, ntx, tiles,
-                                                                                 d.last_bin_only < 0 ? 1 : 0);
+  const int ntx = (d.nx + TILE_X - 1) / TILE_X, ntz = (d.nz + TILE_Z - 1) / TILE_Z;
+  // each launch draws tiles from a fresh counter
+  cudaError_t e = cudaMemsetAsync(d.counters + 3, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  sa_pick(d.wtx_id, d.wrx_id)<<<grid, NTHREADS, sa_smem(d), s>>>(d, image, wtx, wrx, ntx, ntz,
+                                                                  d.last_bin_only < 0 ? 1 : 0);
   return cudaGetLastError();
 }
 
