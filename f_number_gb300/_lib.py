@@ -16,7 +16,7 @@ EXPORTS = (
     "fnum_f_number_values", "fnum_window_value", "fnum_das_pw", "fnum_das_sa", "fnum_pw_plan_create",
     "fnum_sa_plan_create", "fnum_plan_execute", "fnum_plan_execute_dft", "fnum_plan_execute_beamform",
     "fnum_plan_info_get", "fnum_plan_f_numbers", "fnum_plan_destroy", "fnum_diag_fp32_peak",
-    "fnum_das_pw_noalloc",
+    "fnum_das_pw_noalloc", "fnum_bmode",
 )
 
 # status codes (fnum_status)
@@ -156,6 +156,8 @@ def lib():
     L.fnum_das_pw_noalloc.restype = C.c_int
     L.fnum_das_pw_noalloc.argtypes = [C.POINTER(PWDesc), _dp, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                       C.c_void_p]
+    L.fnum_bmode.restype = C.c_int
+    L.fnum_bmode.argtypes = [C.c_void_p, C.c_longlong, C.c_int, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
     if L.fnum_abi_version() != 1:
         raise LibraryNotBuilt("libfnum.so ABI version mismatch")
     _lib = L

@@ -511,3 +511,27 @@ class SAPlan(_Plan):
         inf = self.info()
         self.n_x, self.n_z, self.n_bins = inf["n_x"], inf["n_z"], inf["n_bins"]
         self.n_out = 1
+
+
+# ---------------------------------------------------------------------------
+# post-processing on the device
+# ---------------------------------------------------------------------------
+def bmode(image, floor_db=float("-inf"), stream=None):
+    """B-mode image in dB on the device: 20 log10(|sum_a I_a| / max |sum_a I_a|),
+    clamped below at floor_db.  image: complex64 CUDA tensor [n_images, N_x, N_z]
+    (per-angle images are compounded coherently first, examples.m:78) or
+    [N_x, N_z].  Returns (dB tensor [N_x, N_z] float32, max |I| as a 0-d tensor).
+    Replaces the host-side steps of the reference's example script
+    (examples.m:88,96)."""
+    import torch
+    img = image if image.dim() == 3 else image.unsqueeze(0)
+    if img.dtype != torch.complex64 or not img.is_cuda:
+        raise TypeError("bmode expects a complex64 CUDA tensor")
+    img = img.contiguous()
+    n_img, nx, nz = img.shape
+    db = torch.empty((nx, nz), dtype=torch.float32, device=img.device)
+    mx = torch.empty((), dtype=torch.float32, device=img.device)
+    st = _Plan._stream_ptr(stream if stream is not None else torch.cuda.current_stream(img.device))
+    _lib.check(_lib.lib().fnum_bmode(img.data_ptr(), nx * nz, n_img, float(floor_db), db.data_ptr(), mx.data_ptr(),
+                                     st))
+    return db, mx

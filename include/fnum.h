@@ -232,6 +232,18 @@ int fnum_das_pw_noalloc(const fnum_pw_desc* desc, const double* steering_angles,
 int fnum_plan_f_numbers(const fnum_plan* plan, double* values);
 int fnum_plan_destroy(fnum_plan* plan);
 
+/* --- post-processing on the device ---------------------------------------- */
+/* B-mode image: d_db[i] = max(20 log10(|s_i| / max_j |s_j|), floor_db) with
+   s_i = sum over the n_images images of d_image (float2 [n_images][n_voxels]),
+   i.e. coherent compounding over angles and log compression in one call.
+   Replaces the host-side steps of the reference's example script
+   (examples.m:78 sums the per-angle images, examples.m:88,96 take
+   20 log10(abs(image) / max(abs(image(:))))).  d_max_abs receives max_j |s_j|
+   (one float on the device).  floor_db = -INFINITY keeps every value; an
+   all-zero image gives floor_db everywhere (the script would give NaN). */
+int fnum_bmode(const void* d_image, long long n_voxels, int n_images, float floor_db, float* d_db,
+               float* d_max_abs, void* stream);
+
 /* --- diagnostics (no counterpart in the reference) ---------------------- */
 /* sustained FP32 FMA throughput of the device (TFLOP/s, 2 flops per FMA): the
    roofline denominator of the fused kernels, which are bound by the FP32 pipe */
