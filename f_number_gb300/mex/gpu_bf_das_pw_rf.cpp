@@ -3,10 +3,12 @@
 // Drop-in for the reference's +cuda/gpu_bf_das_pw_rf.cu (mexFunction at line
 // 110): same 8-15 inputs, same <= 2 outputs (single complex image, single
 // weights), same error identifiers.  Parameter objects are read the way the
-// reference reads them: windows by class (gpu_bf_helper_functions.cu:56-97),
-// F-numbers through their MATLAB compute_values method on the band's
-// normalised pitches (gpu_bf_helper_functions.cu:35-51), so user-defined
-// F-number subclasses keep working.
+// reference reads them: windows by class (gpu_bf_helper_functions.cu:56-97).
+// F-numbers of the built-in classes are tabulated by the library itself
+// (fnum_mex_objects.h), so the call makes no MATLAB callback; other classes,
+// such as user-defined subclasses, go through their MATLAB compute_values
+// method on the band's normalised pitches, as in the reference
+// (gpu_bf_helper_functions.cu:35-51).
 //
 // Build (MATLAB): mex -R2017b gpu_bf_das_pw_rf.cpp -I<repo>/include -L<repo>/f_number_gb300 -lfnum
 #include <math.h>
@@ -15,6 +17,7 @@
 #include <vector>
 
 #include "fnum.h"
+#include "fnum_mex_objects.h"
 #include "mex.h"
 
 namespace {
@@ -105,7 +108,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
       fail("InvalidWindow", "Receive window must be a single object of the class windows.window!");
     if (!window_of(prhs[10], &d.window)) fail("InvalidWindow", "Could not read window parameters!");
   }
-  // F-number: the MATLAB object's own compute_values on the band (user subclasses included)
+  // F-number table on the band: native for the built-in classes, else the object's compute_values
   d.f_number.kind = FNUM_F_DEFAULT;
   std::vector<double> fvals;
   if (nrhs >= 12 && !mxIsEmpty(prhs[11])) {
@@ -117,12 +120,21 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
     if (s != FNUM_OK) fail_status(s);
     mxArray* pl = mxCreateDoubleMatrix(kub - klb + 1, 1, mxREAL);
     for (int k = klb; k <= kub; ++k) mxGetPr(pl)[k - klb] = d.element_pitch * k * d.f_s / (N * d.c_0);
-    mxArray* lhs = nullptr;
-    mxArray* rhs[2] = {mxDuplicateArray(prhs[11]), pl};
-    mexCallMATLAB(1, &lhs, 2, rhs, "compute_values");
-    fvals.assign(mxGetPr(lhs), mxGetPr(lhs) + mxGetNumberOfElements(lhs));
-    mxDestroyArray(lhs);
-    mxDestroyArray(rhs[0]);
+    fnum_f_number nf;
+    if (fnum_mex::native_f_number(prhs[11], &nf)) {
+      // built-in class: the library's own table, no MATLAB callback
+      fvals.resize(kub - klb + 1);
+      const int st = fnum_f_number_values(&nf, mxGetPr(pl), kub - klb + 1, fvals.data());
+      if (st != FNUM_OK) fail_status(st);
+    } else {
+      mxArray* lhs = nullptr;
+      mxArray* rhs[2] = {mxDuplicateArray(prhs[11]), mxDuplicateArray(pl)};
+      mexCallMATLAB(1, &lhs, 2, rhs, "compute_values");
+      fvals.assign(mxGetPr(lhs), mxGetPr(lhs) + mxGetNumberOfElements(lhs));
+      mxDestroyArray(lhs);
+      mxDestroyArray(rhs[0]);
+      mxDestroyArray(rhs[1]);
+    }
     mxDestroyArray(pl);
     d.f_number_values = fvals.data();
     d.n_f_number_values = (int)fvals.size();

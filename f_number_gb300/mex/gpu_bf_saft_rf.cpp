@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "fnum.h"
+#include "fnum_mex_objects.h"
 #include "mex.h"
 
 namespace {
@@ -65,7 +66,8 @@ void read_window(int nrhs, const mxArray* prhs[], int i, fnum_window* w, const c
   }
 }
 
-// F-number values on the band through the object's MATLAB compute_values
+// F-number values on the band: native for the built-in classes (fnum_mex_objects.h),
+// else through the object's MATLAB compute_values
 void read_f_number(int nrhs, const mxArray* prhs[], int i, const fnum_sa_desc& d, std::vector<double>& v) {
   int N = 0, klb = 0, kub = 0;
   const int s = fnum_band(d.positions_z, d.n_z, d.n_samples, d.n_elements, d.f_s, d.element_width, d.element_pitch,
@@ -76,12 +78,21 @@ void read_f_number(int nrhs, const mxArray* prhs[], int i, const fnum_sa_desc& d
   if (nrhs > i && !mxIsEmpty(prhs[i])) {
     if (!(isa(prhs[i], "f_numbers.f_number") && mxIsScalar(prhs[i])))
       fail("InvalidFNumber", "F-number must be a single object of the class f_numbers.f_number!");
-    mxArray* lhs = nullptr;
-    mxArray* rhs[2] = {mxDuplicateArray(prhs[i]), pl};
-    mexCallMATLAB(1, &lhs, 2, rhs, "compute_values");
-    v.assign(mxGetPr(lhs), mxGetPr(lhs) + mxGetNumberOfElements(lhs));
-    mxDestroyArray(lhs);
-    mxDestroyArray(rhs[0]);
+    fnum_f_number nf;
+    if (fnum_mex::native_f_number(prhs[i], &nf)) {
+      // built-in class: the library's own table, no MATLAB callback
+      v.resize(kub - klb + 1);
+      const int st = fnum_f_number_values(&nf, mxGetPr(pl), kub - klb + 1, v.data());
+      if (st != FNUM_OK) fail_status(st);
+    } else {
+      mxArray* lhs = nullptr;
+      mxArray* rhs[2] = {mxDuplicateArray(prhs[i]), mxDuplicateArray(pl)};
+      mexCallMATLAB(1, &lhs, 2, rhs, "compute_values");
+      v.assign(mxGetPr(lhs), mxGetPr(lhs) + mxGetNumberOfElements(lhs));
+      mxDestroyArray(lhs);
+      mxDestroyArray(rhs[0]);
+      mxDestroyArray(rhs[1]);
+    }
   } else {
     fnum_f_number def;
     memset(&def, 0, sizeof(def));
