@@ -16,8 +16,11 @@ EXPORTS = (
     "fnum_f_number_values", "fnum_window_value", "fnum_das_pw", "fnum_das_sa", "fnum_pw_plan_create",
     "fnum_sa_plan_create", "fnum_plan_execute", "fnum_plan_execute_dft", "fnum_plan_execute_beamform",
     "fnum_plan_info_get", "fnum_plan_f_numbers", "fnum_plan_destroy", "fnum_diag_fp32_peak",
-    "fnum_das_pw_noalloc", "fnum_bmode",
+    "fnum_das_pw_noalloc", "fnum_bmode", "fnum_plan_autotune", "fnum_batch_create", "fnum_batch_execute",
+    "fnum_batch_frame_times", "fnum_batch_destroy",
 )
+
+ABI_VERSION = 2   # FNUM_ABI_VERSION of include/fnum.h
 
 # status codes (fnum_status)
 OK = 0
@@ -90,6 +93,7 @@ class PlanInfo(C.Structure):
         ("scratch_bytes", C.c_longlong),
         ("scale", C.c_double),
         ("executed_terms", C.c_longlong),
+        ("kernel_variant", C.c_int), ("grid", C.c_int),
     ]
 
 
@@ -156,9 +160,21 @@ def lib():
     L.fnum_das_pw_noalloc.restype = C.c_int
     L.fnum_das_pw_noalloc.argtypes = [C.POINTER(PWDesc), _dp, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                       C.c_void_p]
+    L.fnum_plan_autotune.restype = C.c_int
+    L.fnum_plan_autotune.argtypes = [C.c_void_p, C.c_void_p, C.c_int, _ip, _fp]
+    L.fnum_batch_create.restype = C.c_int
+    L.fnum_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p), _ip,
+                                    C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int,
+                                    C.POINTER(C.c_void_p)]
+    L.fnum_batch_execute.restype = C.c_int
+    L.fnum_batch_execute.argtypes = [C.c_void_p, C.c_void_p]
+    L.fnum_batch_frame_times.restype = C.c_int
+    L.fnum_batch_frame_times.argtypes = [C.c_void_p, _fp]
+    L.fnum_batch_destroy.restype = C.c_int
+    L.fnum_batch_destroy.argtypes = [C.c_void_p]
     L.fnum_bmode.restype = C.c_int
     L.fnum_bmode.argtypes = [C.c_void_p, C.c_longlong, C.c_int, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
-    if L.fnum_abi_version() != 1:
+    if L.fnum_abi_version() != ABI_VERSION:
         raise LibraryNotBuilt("libfnum.so ABI version mismatch")
     _lib = L
     return L

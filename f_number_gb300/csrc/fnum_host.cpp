@@ -411,6 +411,7 @@ struct fnum_plan {
   int device = 0;
   int n_out = 1;
   int grid = 0;
+  int max_grid = 0;   // the segment scratch holds this many blocks
   Band band{};
   fnum::PWDev pw{};
   fnum::SADev sa{};
@@ -625,10 +626,13 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
   {
     int bps = 0;
     P->grid = fnum::pw_fused_grid(D, &bps);
+    // scratch for the largest grid of any kernel variant, so the autotuner may switch
+    P->max_grid = fnum::pw_fused_max_grid(D);
     int4* seg;
-    if ((s = P->alloc(&seg, (size_t)P->grid * fnum::NTHREADS * D.seg_cap * fnum::PW_SEG_INT4))) goto fail;
+    if ((s = P->alloc(&seg, (size_t)P->max_grid * fnum::NTHREADS * D.seg_cap * fnum::PW_SEG_INT4))) goto fail;
     D.seg = seg;
-    P->info.scratch_bytes = (long long)P->grid * fnum::NTHREADS * D.seg_cap * fnum::PW_SEG_INT4 * (long long)sizeof(int4);
+    P->info.scratch_bytes =
+        (long long)P->max_grid * fnum::NTHREADS * D.seg_cap * fnum::PW_SEG_INT4 * (long long)sizeof(int4);
   }
   {
     cudaError_t e = fnum::launch_twiddles(P->tw, b.N, 0);
@@ -737,6 +741,7 @@ int make_sa_plan(const fnum_sa_desc* d, int flags, fnum_plan** out) {
   {
     int bps = 0;
     P->grid = fnum::sa_fused_grid(D, &bps);
+    P->max_grid = P->grid;
     int4* seg;
     if ((s = P->alloc(&seg, (size_t)P->grid * fnum::NTHREADS * D.seg_cap * fnum::SA_SEG_INT4))) goto fail;
     D.seg = seg;
@@ -975,6 +980,8 @@ int fnum_plan_info_get(const fnum_plan* plan, fnum_plan_info* info) {
   info->active_terms = (long long)c[0];
   info->zero_weight_bins = (long long)c[1];
   info->executed_terms = (long long)c[4];
+  info->kernel_variant = plan->kind == 0 ? fnum::pw_variant_of(plan->pw) : 0;
+  info->grid = plan->grid;
   if (c[2] & fnum::ERR_SEG_OVERFLOW) return FNUM_ERR_INTERNAL;
   return FNUM_OK;
 }
@@ -1049,6 +1056,200 @@ int fnum_das_sa(const fnum_sa_desc* desc, const double* data_rf, int flags, floa
   }
   const size_t rf_count = (size_t)desc->n_elements * desc->n_elements * desc->n_samples;
   return run_host(g_sa_cache.plan, data_rf, rf_count, image_re, image_im, weights_tx, weights_rx);
+}
+
+// ---------------------------------------------------------------------------
+// autotuning and batches (no counterpart in the reference, which beamforms one
+// angle per gateway call)
+// ---------------------------------------------------------------------------
+int fnum_plan_autotune(fnum_plan* plan, const void* d_rf, int rf_is_double, int* variant, float* ms) {
+  if (!plan || !d_rf) return FNUM_ERR_ARGUMENT;
+  FNUM_CUDA(cudaSetDevice(plan->device));
+  if (plan->kind != 0) {  // the synthetic-aperture kernel has one variant
+    if (variant) *variant = 0;
+    if (ms) *ms = 0.0f;
+    return FNUM_OK;
+  }
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  float2* img = nullptr;
+  int s = FNUM_OK;
+  const size_t n_img = (size_t)plan->n_out * plan->pw.nx * plan->pw.nz;
+  const int v0 = plan->pw.variant, g0 = plan->grid;
+  float best = 3.0e38f;
+  int best_v = fnum::pw_variant_of(plan->pw), best_g = plan->grid;
+  cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) e = cudaMalloc(&img, n_img * sizeof(float2));
+  if (e != cudaSuccess) {
+    s = cuda_status(e);
+    goto done;
+  }
+  if ((s = plan_dft(plan, d_rf, rf_is_double, st))) goto done;
+  for (int v = 1; v <= fnum::pw_variant_count(); ++v) {
+    plan->pw.variant = v;
+    plan->grid = std::min(fnum::pw_fused_grid(plan->pw, nullptr), plan->max_grid);
+    if ((s = plan_beamform(plan, img, nullptr, nullptr, st))) goto done;  // warm-up
+    float t = 0.0f;
+    e = cudaEventRecord(e0, st);
+    for (int r = 0; r < 2 && e == cudaSuccess && !s; ++r) s = plan_beamform(plan, img, nullptr, nullptr, st);
+    if (s) goto done;
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    if (e != cudaSuccess) {
+      s = cuda_status(e);
+      goto done;
+    }
+    if (t < best) {
+      best = t;
+      best_v = v;
+      best_g = plan->grid;
+    }
+  }
+done:
+  if (s) {
+    plan->pw.variant = v0;
+    plan->grid = g0;
+  } else {
+    plan->pw.variant = best_v;
+    plan->grid = best_g;
+    if (variant) *variant = best_v;
+    if (ms) *ms = 0.5f * best;
+  }
+  if (img) cudaFree(img);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  (void)cudaGetLastError();
+  return s;
+}
+
+struct fnum_batch {
+  int device = 0;
+  int n = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t start = nullptr;
+  std::vector<cudaEvent_t> done;   // per frame, recorded when the frame's image is complete
+  ~fnum_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (start) cudaEventDestroy(start);
+    for (cudaEvent_t ev : done)
+      if (ev) cudaEventDestroy(ev);
+  }
+};
+
+int fnum_batch_create(fnum_plan* const* plans, int n, const void* const* d_rf, const int* rf_is_double,
+                      void* const* d_images, float* const* d_weights, float* const* d_weights_rx, int n_streams,
+                      fnum_batch** batch) {
+  if (!plans || n <= 0 || !d_rf || !d_images || !batch) return FNUM_ERR_ARGUMENT;
+  *batch = nullptr;
+  for (int i = 0; i < n; ++i) {
+    if (!plans[i] || !d_rf[i] || !d_images[i]) return FNUM_ERR_ARGUMENT;
+    if (plans[i]->device != plans[0]->device) return FNUM_ERR_ARGUMENT;
+    for (int j = 0; j < i; ++j)
+      if (plans[j] == plans[i]) return FNUM_ERR_ARGUMENT;  // a plan's buffers serve one frame at a time
+  }
+  FNUM_CUDA(cudaSetDevice(plans[0]->device));
+  const int k = std::max(1, std::min(n_streams, n));
+  // longest frames first, each to the branch with the least work so far
+  std::vector<int> order(n), branch(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return plans[a]->info.terms > plans[b]->info.terms; });
+  std::vector<double> load(k, 0.0);
+  for (int f : order) {
+    const int b = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    branch[f] = b;
+    load[b] += (double)plans[f]->info.terms;
+  }
+  fnum_batch* B = new (std::nothrow) fnum_batch;
+  if (!B) return FNUM_ERR_ARGUMENT;
+  B->device = plans[0]->device;
+  B->n = n;
+  B->done.assign(n, nullptr);
+  std::vector<cudaStream_t> st(k, nullptr);
+  std::vector<cudaEvent_t> fj(k, nullptr);  // fork (0) and joins (1..k-1)
+  int s = FNUM_OK;
+  bool capturing = false;
+  cudaError_t e = cudaEventCreate(&B->start);
+  for (int i = 0; i < n && e == cudaSuccess; ++i) e = cudaEventCreate(&B->done[i]);
+  for (int i = 0; i < k && e == cudaSuccess; ++i) e = cudaStreamCreateWithFlags(&st[i], cudaStreamNonBlocking);
+  for (int i = 0; i < k && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&fj[i], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(st[0], cudaStreamCaptureModeThreadLocal);
+  capturing = (e == cudaSuccess);
+  if (e == cudaSuccess) e = cudaEventRecordWithFlags(B->start, st[0], cudaEventRecordExternal);
+  if (e == cudaSuccess) e = cudaEventRecord(fj[0], st[0]);
+  for (int i = 1; i < k && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(st[i], fj[0], 0);
+  if (e != cudaSuccess) s = cuda_status(e);
+  for (int f : order) {
+    if (s) break;
+    cudaStream_t q = st[branch[f]];
+    if ((s = plan_dft(plans[f], d_rf[f], rf_is_double ? rf_is_double[f] : 0, q))) break;
+    if ((s = plan_beamform(plans[f], d_images[f], d_weights ? d_weights[f] : nullptr,
+                           d_weights_rx ? d_weights_rx[f] : nullptr, q)))
+      break;
+    e = cudaEventRecordWithFlags(B->done[f], q, cudaEventRecordExternal);
+    if (e != cudaSuccess) s = cuda_status(e);
+  }
+  for (int i = 1; i < k && !s; ++i) {
+    e = cudaEventRecord(fj[i], st[i]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st[0], fj[i], 0);
+    if (e != cudaSuccess) s = cuda_status(e);
+  }
+  if (capturing) {
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(st[0], &g);
+    if (!s && e != cudaSuccess) s = cuda_status(e);
+    if (s) {
+      if (g) cudaGraphDestroy(g);
+    } else {
+      B->graph = g;
+      e = cudaGraphInstantiate(&B->exec, g, 0);
+      if (e != cudaSuccess) s = cuda_status(e);
+    }
+  }
+  for (int i = 0; i < k; ++i) {
+    if (fj[i]) cudaEventDestroy(fj[i]);
+    if (st[i]) cudaStreamDestroy(st[i]);
+  }
+  (void)cudaGetLastError();
+  if (s) {
+    delete B;
+    return s;
+  }
+  *batch = B;
+  return FNUM_OK;
+}
+
+int fnum_batch_execute(fnum_batch* batch, void* stream) {
+  if (!batch || !batch->exec) return FNUM_ERR_ARGUMENT;
+  FNUM_CUDA(cudaSetDevice(batch->device));
+  FNUM_CUDA(cudaGraphLaunch(batch->exec, (cudaStream_t)stream));
+  return FNUM_OK;
+}
+
+int fnum_batch_frame_times(const fnum_batch* batch, float* ms) {
+  if (!batch || !ms) return FNUM_ERR_ARGUMENT;
+  FNUM_CUDA(cudaSetDevice(batch->device));
+  for (int i = 0; i < batch->n; ++i) {
+    cudaError_t e = cudaEventElapsedTime(&ms[i], batch->start, batch->done[i]);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      return cuda_status(e);
+    }
+  }
+  return FNUM_OK;
+}
+
+int fnum_batch_destroy(fnum_batch* batch) {
+  if (!batch) return FNUM_OK;
+  cudaSetDevice(batch->device);
+  delete batch;
+  return FNUM_OK;
 }
 
 }  // extern "C"

@@ -33,6 +33,7 @@ struct PWDev {
   int seg_cap;         // segment entries per voxel
   int flush_chunks;    // flush Horner accumulators every flush_chunks * KCHUNK bins
   float scale;         // 2 / N_dft
+  int variant;         // fused kernel variant, 0 = by angle count (launch_pw_fused)
   // per column [nx]
   const dfl* col_u;    // K_u x
   const dfl* col_p;    // M + x / pitch
@@ -96,7 +97,10 @@ cudaError_t launch_dft_pw(const void* rf, int is_double, int na, int ne, int nt,
                           int k_lb, int K, float2* X, cudaStream_t s);
 cudaError_t launch_dft_sa(const void* rf, int is_double, int nsig, int nt, const float2* tw, int N, int k_lb,
                           int K, float2* X, cudaStream_t s);
-int pw_fused_grid(const PWDev& d, int* blocks_per_sm);
+int pw_fused_grid(const PWDev& d, int* blocks_per_sm);   // grid of d's variant, all blocks resident
+int pw_fused_max_grid(const PWDev& d);                     // largest of those over the variants
+int pw_variant_count();
+int pw_variant_of(const PWDev& d);
 int sa_fused_grid(const SADev& d, int* blocks_per_sm);
 cudaError_t launch_pw_fused(const PWDev& d, int grid, float2* image, float* weights, cudaStream_t s);
 cudaError_t launch_pw_plain(const PWDev& d, float2* image, float* weights, cudaStream_t s);

@@ -737,15 +737,32 @@ static pw_kernel_t pw_pick_win(int window_id) {
   }
 }
 
-static pw_kernel_t pw_pick(int na, int window_id) {
-  if (na >= 11) return pw_pick_win<1, 11>(window_id);
-  if (na >= 4) return pw_pick_win<2, 4>(window_id);
-  if (na >= 2) return pw_pick_win<2, 2>(window_id);
-  return pw_pick_win<4, 1>(window_id);
+// Kernel variants: how many elements (EPT) and angles (NA) one pass carries.
+//   1: EPT 1 x NA 11   2: EPT 2 x NA 4   3: EPT 2 x NA 2   4: EPT 4 x NA 1
+// Angles beyond NA run as further passes inside the launch.  PWDev::variant
+// 0 picks by the angle count; a plan's autotuner may set another.
+static pw_kernel_t pw_variant_kernel(int v, int window_id) {
+  switch (v) {
+    case 1: return pw_pick_win<1, 11>(window_id);
+    case 2: return pw_pick_win<2, 4>(window_id);
+    case 3: return pw_pick_win<2, 2>(window_id);
+    default: return pw_pick_win<4, 1>(window_id);
+  }
 }
+static int pw_default_variant(int na) {
+  if (na >= 11) return 1;
+  if (na >= 4) return 2;
+  if (na >= 2) return 3;
+  return 4;
+}
+static pw_kernel_t pw_pick(const PWDev& d) {
+  return pw_variant_kernel(d.variant > 0 ? d.variant : pw_default_variant(d.na), d.window_id);
+}
+int pw_variant_count() { return 4; }
+int pw_variant_of(const PWDev& d) { return d.variant > 0 ? d.variant : pw_default_variant(d.na); }
 
 int pw_fused_grid(const PWDev& d, int* blocks_per_sm) {
-  pw_kernel_t fn = pw_pick(d.na, d.window_id);
+  pw_kernel_t fn = pw_pick(d);
   int dev = 0, nsm = 0, bps = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -756,13 +773,23 @@ int pw_fused_grid(const PWDev& d, int* blocks_per_sm) {
   return tiles < nsm * bps ? tiles : nsm * bps;
 }
 
+int pw_fused_max_grid(const PWDev& d) {
+  int g = 0;
+  for (int v = 1; v <= pw_variant_count(); ++v) {
+    PWDev t = d;
+    t.variant = v;
+    g = max(g, pw_fused_grid(t, nullptr));
+  }
+  return g;
+}
+
 cudaError_t launch_pw_fused(const PWDev& d, int grid, float2* image, float* weights, cudaStream_t s) {
   const int ntx = (d.nx + TILE_X - 1) / TILE_X, ntz = (d.nz + TILE_Z - 1) / TILE_Z;
   const size_t smem = (size_t)d.ne * (sizeof(int) + 2 * sizeof(dfl));
   // each launch draws tiles from a fresh counter
   cudaError_t e = cudaMemsetAsync(d.counters + 3, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
-  pw_pick(d.na, d.window_id)<<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, ntz);
+  pw_pick(d)<<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, ntz);
   return cudaGetLastError();
 }
 // ---------------------------------------------------------------------------

@@ -441,6 +441,16 @@ class _Plan:
             weights_rx.data_ptr() if weights_rx is not None else None, self._stream_ptr(stream)), self._saft)
         return out
 
+    def autotune(self, rf):
+        """Times the fused kernel's variants on this plan's data (fnum_plan_autotune)
+        and keeps the fastest.  Returns (variant, beamform ms of the choice)."""
+        import torch
+        v = _lib.C.c_int(0)
+        ms = _lib.C.c_float(0.0)
+        _lib.check(_lib.lib().fnum_plan_autotune(self._ptr, rf.data_ptr(), int(rf.dtype == torch.float64),
+                                                 _lib.C.byref(v), _lib.C.byref(ms)), self._saft)
+        return v.value, ms.value
+
 
 class PWPlan(_Plan):
     """Plane-wave plan: one or many steering angles with the same geometry."""
@@ -475,6 +485,7 @@ class PWPlan(_Plan):
         self._ptr = ptr
         inf = self.info()
         self.n_x, self.n_z, self.n_bins = inf["n_x"], inf["n_z"], inf["n_bins"]
+        self.n_elements, self.n_angles = inf["n_elements"], inf["n_angles"]
         self.n_out = 1 if compound else self._angles.size
 
 
@@ -535,3 +546,47 @@ def bmode(image, floor_db=float("-inf"), stream=None):
     _lib.check(_lib.lib().fnum_bmode(img.data_ptr(), nx * nz, n_img, float(floor_db), db.data_ptr(), mx.data_ptr(),
                                      st))
     return db, mx
+
+
+class Batch:
+    """Frames of uneven shape in one CUDA graph (fnum_batch_*).  plans: distinct
+    plans; rfs / images (and weights, optional): the CUDA tensors each frame
+    reads and writes, bound for the batch's life.  n_streams concurrent branches
+    share the GPU among small frames."""
+
+    def __init__(self, plans, rfs, images, weights=None, n_streams=4):
+        import torch
+        n = len(plans)
+        if not (len(rfs) == len(images) == n) or (weights is not None and len(weights) != n):
+            raise ValueError("plans, rfs, images (and weights) must have the same length")
+        self._keep = (list(plans), list(rfs), list(images), list(weights) if weights is not None else None)
+        P = (_lib.C.c_void_p * n)(*[p._ptr for p in plans])
+        R = (_lib.C.c_void_p * n)(*[r.data_ptr() for r in rfs])
+        D = (_lib.C.c_int * n)(*[int(r.dtype == torch.float64) for r in rfs])
+        I = (_lib.C.c_void_p * n)(*[im.data_ptr() for im in images])
+        W = None if weights is None else (_lib.C.c_void_p * n)(*[w.data_ptr() if w is not None else None
+                                                                   for w in weights])
+        ptr = _lib.C.c_void_p()
+        _lib.check(_lib.lib().fnum_batch_create(P, n, R, D, I, W, None, int(n_streams), _lib.C.byref(ptr)))
+        self._ptr = ptr
+        self.n = n
+
+    def execute(self, stream=None):
+        _lib.check(_lib.lib().fnum_batch_execute(self._ptr, _Plan._stream_ptr(stream)))
+
+    def frame_times(self):
+        """Completion time of each frame in ms from the start of the last execute."""
+        out = np.empty(self.n, dtype=np.float32)
+        _lib.check(_lib.lib().fnum_batch_frame_times(self._ptr, out.ctypes.data_as(_lib.C.POINTER(_lib.C.c_float))))
+        return out
+
+    def close(self):
+        if getattr(self, "_ptr", None) is not None:
+            _lib.lib().fnum_batch_destroy(self._ptr)
+            self._ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -231,3 +231,40 @@ def saft_128(seed=0, grid=(400, 400), n_samples=3072, n_elements=128, f_bounds=N
         sc = random_points(rng, 50, (-19e-3, 19e-3), (3e-3, 40e-3))
         wl.rf = sa_rf(rng, arr, sc, n_samples, wl.f_s, wl.c, snr_db=20.0)
     return wl
+
+
+def batch_64(seed=0, n_frames=64, with_rf=True, n_points=60, n_speckle=240):
+    """Plane-wave frames of uneven shape: per frame, elements from {64, 96, 128,
+    192}, angles from {1, 5, 11, 31} (0 deg, or evenly spaced over -10..10 deg),
+    samples from {1024, 2048, 4096}, a square grid of 128 .. 768 voxels per side
+    at pitch / 5 spacing starting 5 mm deep, 2-7 MHz, Hann window, angle_lb(60,
+    1.5).  RF from the seeded point + speckle model with a smaller scatterer
+    count than the single-frame workloads (60 points + 240 speckle scatterers),
+    so that 64 frames synthesise in seconds; the beamformer's cost does not
+    depend on the RF content."""
+    rng = np.random.default_rng(seed)
+    frames = []
+    for f in range(n_frames):
+        ne = int(rng.choice([64, 96, 128, 192]))
+        na = int(rng.choice([1, 5, 11, 31]))
+        nt = int(rng.choice([1024, 2048, 4096]))
+        side = int(rng.integers(128, 769))
+        pitch = 0.3048e-3
+        arr = LinearArray(ne, pitch, 0.918 * pitch)
+        dx = pitch / 5.0
+        px = (np.arange(side) - (side - 1) / 2.0) * dx
+        pz = 5e-3 + np.arange(side) * dx
+        angles = np.zeros(1) if na == 1 else np.deg2rad(np.linspace(-10.0, 10.0, na))
+        wl = PWWorkload("batch_%02d_%del_%dang_%dsmp_%dx%d" % (f, ne, na, nt, side, side), arr, 20e6, 1540.0, nt,
+                        angles, px, pz, (2e6, 7e6), ("hann", 0.0),
+                        {"kind": "grating.angle_lb", "angle_lb_deg": 60.0, "F_number_ub": 1.5, "distance_deg": 10.0})
+        if with_rf:
+            half = 0.5 * ne * pitch
+            xr = (-half, half)
+            zr = (5e-3, min(5e-3 + nt / 20e6 * 1540.0 / 2.0, 5e-3 + side * dx))
+            pts = random_points(rng, n_points, xr, zr)
+            spk = random_points(rng, n_speckle, xr, zr)
+            spk.amp = rng.standard_normal(n_speckle)
+            wl.rf = pw_rf(rng, arr, merge(pts, spk), wl.angles, nt, wl.f_s, wl.c, snr_db=30.0)
+        frames.append(wl)
+    return frames

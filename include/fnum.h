@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define FNUM_ABI_VERSION 1
+#define FNUM_ABI_VERSION 2
 
 typedef enum fnum_status {
   FNUM_OK = 0,
@@ -186,6 +186,8 @@ typedef struct fnum_plan_info {
   long long scratch_bytes;         /* device scratch the plan owns */
   double scale;                    /* 2 / N_dft */
   long long executed_terms;        /* recurrence steps the fused kernel ran (>= active_terms), last execute */
+  int kernel_variant;              /* PW fused kernel variant (1..4, see fnum_plan_autotune); 0 for SA */
+  int grid;                        /* blocks of the fused kernel's launch */
 } fnum_plan_info;
 
 int fnum_pw_plan_create(const fnum_pw_desc* desc, const double* steering_angles, int n_angles,
@@ -228,6 +230,34 @@ int fnum_plan_info_get(const fnum_plan* plan, fnum_plan_info* info);
 #define FNUM_NOALLOC_SCRATCH_BYTES (64ull << 20)
 int fnum_das_pw_noalloc(const fnum_pw_desc* desc, const double* steering_angles, int n_angles,
                         const float* d_rf, int flags, void* d_image, float* d_weights, void* stream);
+/* --- autotuning and batches of frames ----------------------------------- */
+/* No counterpart in the reference (one angle per gateway call, nothing kept).
+   fnum_plan_autotune: runs the band DFT of d_rf, then times each fused-kernel
+   variant of a plane-wave plan on it (1: 1 element x 11 angles per pass,
+   2: 2 x 4, 3: 2 x 2, 4: 4 x 1) at full occupancy, and keeps the fastest
+   for the plan's later executes.  It allocates a temporary image and runs on
+   a private stream (not capturable).  variant / ms (the chosen variant's
+   beamform time) may be NULL.  A synthetic-aperture plan has one variant:
+   the call returns variant 0. */
+int fnum_plan_autotune(fnum_plan* plan, const void* d_rf, int rf_is_double, int* variant, float* ms);
+
+/* A batch binds n frames -- distinct plans with their device RF, image and
+   weight buffers -- and captures their band DFTs and beamformers into one CUDA
+   graph.  The frames are spread over n_streams concurrent branches (longest
+   first, each to the least-loaded branch), so small frames share the GPU.
+   Plans and buffers must outlive the batch; d_weights / d_weights_rx / their
+   entries and rf_is_double may be NULL.  fnum_batch_execute launches the
+   graph on `stream`; fnum_batch_frame_times gives, after it completed, each
+   frame's completion time in ms from the batch's start (n values, in the
+   order of `plans`). */
+typedef struct fnum_batch fnum_batch;
+int fnum_batch_create(fnum_plan* const* plans, int n, const void* const* d_rf, const int* rf_is_double,
+                      void* const* d_images, float* const* d_weights, float* const* d_weights_rx, int n_streams,
+                      fnum_batch** batch);
+int fnum_batch_execute(fnum_batch* batch, void* stream);
+int fnum_batch_frame_times(const fnum_batch* batch, float* ms);
+int fnum_batch_destroy(fnum_batch* batch);
+
 /* copies the plan's F table (n_bins values; two tables for SA: tx then rx) */
 int fnum_plan_f_numbers(const fnum_plan* plan, double* values);
 int fnum_plan_destroy(fnum_plan* plan);

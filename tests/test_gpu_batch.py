@@ -1,0 +1,96 @@
+"""Batches of uneven frames in one CUDA graph (fnum_batch_*) and the per-plan
+kernel autotuner (fnum_plan_autotune).
+
+A frame in a batch runs the same kernels as its plan's stand-alone execute, and
+each voxel's arithmetic does not depend on which block or stream processes it,
+so batch images must equal the stand-alone images bit for bit.  The autotuner
+only regroups elements and angles into passes, which changes the rounding of
+the per-group sums: its images stay within 1e-5 relative L2 of the default
+variant's, and within the parity bound of the FP64 oracle."""
+import numpy as np
+import pytest
+
+from f_number_gb300 import _lib, das, f_numbers, synth, windows
+from oracle import fnum_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+PITCH = 0.3048e-3
+FN = f_numbers.grating.angle_lb(60.0, 1.5)
+
+
+def _frame(rng, ne, na, nt, side, compound, gpu):
+    import torch
+    arr = synth.LinearArray(ne, PITCH, 0.918 * PITCH)
+    dx = PITCH / 2
+    px = (np.arange(side) - (side - 1) / 2.0) * dx
+    pz = 6e-3 + np.arange(side) * dx
+    angles = np.zeros(1) if na == 1 else np.deg2rad(np.linspace(-8.0, 8.0, na))
+    sc = synth.random_points(rng, 6, (px[0], px[-1]), (pz[0], pz[-1]))
+    rf = torch.tensor(synth.pw_rf(rng, arr, sc, list(angles), nt, 20e6, 1540.0), dtype=torch.float32, device=gpu)
+    plan = das.PWPlan(px, pz, nt, ne, 20e6, angles, arr.width, arr.pitch, 1540.0, [2e6, 7e6], 0.0, windows.hann(), FN,
+                      compound=compound)
+    return plan, rf, (arr, px, pz, angles)
+
+
+SHAPES = [(32, 1, 512, 24, True), (48, 5, 1024, 40, False), (64, 11, 1024, 32, True), (40, 3, 768, 28, True),
+          (56, 2, 512, 36, False), (24, 31, 512, 20, True)]
+
+
+def test_batch_equals_standalone_plans(gpu):
+    import torch
+    rng = np.random.default_rng(11)
+    frames = [_frame(rng, *s, gpu) for s in SHAPES]
+    plans = [f[0] for f in frames]
+    rfs = [f[1] for f in frames]
+    expect, expect_w = [], []
+    for p, rf in zip(plans, rfs):
+        w = torch.empty((p.n_x, p.n_z), dtype=torch.float32, device=gpu)
+        expect.append(p.execute(rf, weights=w).clone())
+        expect_w.append(w.clone())
+    images = [torch.full_like(e, float("nan")) for e in expect]
+    weights = [torch.full_like(w, float("nan")) if i % 2 == 0 else None for i, w in enumerate(expect_w)]
+    batch = das.Batch(plans, rfs, images, weights=weights, n_streams=3)
+    for rep in range(2):                        # the graph is relaunched: same results
+        for im in images:
+            im.fill_(float("nan"))
+        batch.execute()
+        torch.cuda.synchronize()
+        for i, (im, e) in enumerate(zip(images, expect)):
+            assert torch.equal(im, e), (rep, i)
+            if weights[i] is not None:
+                assert torch.equal(weights[i], expect_w[i])
+        t = batch.frame_times()
+        assert np.all(np.isfinite(t)) and np.all(t > 0)
+    batch.close()
+    for p in plans:
+        p.close()
+
+
+def test_batch_rejects_a_plan_twice(gpu):
+    import torch
+    rng = np.random.default_rng(12)
+    plan, rf, _ = _frame(rng, 32, 1, 512, 16, True, gpu)
+    im = [torch.empty((1, plan.n_x, plan.n_z), dtype=torch.complex64, device=gpu) for _ in range(2)]
+    with pytest.raises(_lib.FNumError):
+        das.Batch([plan, plan], [rf, rf], im)
+    plan.close()
+
+
+@pytest.mark.parametrize("na", [1, 5, 11])
+def test_autotune_keeps_results(gpu, na):
+    rng = np.random.default_rng(13 + na)
+    plan, rf, (arr, px, pz, angles) = _frame(rng, 48, na, 1024, 32, True, gpu)
+    ref = plan.execute(rf).cpu().numpy()
+    v, ms = plan.autotune(rf)
+    assert 1 <= v <= 4 and ms > 0
+    assert plan.info()["kernel_variant"] == v
+    img = plan.execute(rf).cpu().numpy()
+    assert np.linalg.norm(img - ref) / np.linalg.norm(ref) < 1e-5
+    # against the FP64 oracle (compounded MEX semantics, image [z][x])
+    rf_np = rf.cpu().numpy().astype(np.float64)
+    o = sum(O.das_pw_mex(px, pz, rf_np[a].T, 20e6, angles[a], arr.width, arr.pitch, 1540.0, (2e6, 7e6), 0.0,
+                         ("hann", 0.0), FN.spec(), "on")[0] for a in range(na))
+    got = img[0].T
+    assert np.linalg.norm(got - o) / np.linalg.norm(o) < 1e-4
+    plan.close()
