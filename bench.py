@@ -43,9 +43,12 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--grid", type=int, default=512, help="voxels per side (512 = the benchmark grid; smaller "
                     "sizes keep the same 0.06 mm spacing, for profiling)")
-    ap.add_argument("--workload", default="cpwc", choices=["cpwc", "saft"],
-                    help="cpwc (default, the headline) or saft: 128 x 128 synthetic aperture, 3072 samples at "
-                    "40 MHz, 400 x 400 voxels, directivity F-number, boxcar windows")
+    ap.add_argument("--workload", default="cpwc", choices=["cpwc", "saft", "batch"],
+                    help="cpwc (default, the headline); saft: 128 x 128 synthetic aperture, 3072 samples at "
+                    "40 MHz, 400 x 400 voxels, directivity F-number, boxcar windows; batch: 64 plane-wave frames "
+                    "of uneven shape in one CUDA graph")
+    ap.add_argument("--frames", type=int, default=64, help="batch: frames per batch")
+    ap.add_argument("--no-autotune", action="store_true", help="batch: keep each plan's default kernel variant")
     ap.add_argument("--band", default="full", choices=["full", "2-7"],
                     help="saft band: the gateway default [DBL_MIN, f_s/2] or 2-7 MHz")
     return ap.parse_args()
@@ -373,11 +376,93 @@ def run_saft(args):
     plan.close()
 
 
+# ---------------------------------------------------------------------------
+# batched workload: uneven plane-wave frames in one CUDA graph
+# ---------------------------------------------------------------------------
+BATCH_METRIC = "batched PW frames/s (uneven shapes, one CUDA graph)"
+
+
+def run_batch(args):
+    import torch
+    from f_number_gb300 import das, f_numbers, synth, windows
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    t0 = time.perf_counter()
+    frames = synth.batch_64(seed=0, n_frames=args.frames)
+    synth_s = time.perf_counter() - t0
+    fn = f_numbers.grating.angle_lb(60.0, 1.5)
+    plans, rfs, imgs, variants = [], [], [], []
+    for wl in frames:
+        p = das.PWPlan(wl.positions_x, wl.positions_z, wl.n_samples, wl.array.n_elements, wl.f_s, wl.angles,
+                       wl.array.width, wl.array.pitch, wl.c, list(wl.f_bounds), 0.0, windows.hann(), fn, device=0,
+                       compound=True)
+        rf = torch.tensor(wl.rf, dtype=torch.float32, device=dev)
+        if not args.no_autotune:
+            variants.append(p.autotune(rf)[0])
+        plans.append(p)
+        rfs.append(rf)
+        imgs.append(torch.empty((1, p.n_x, p.n_z), dtype=torch.complex64, device=dev))
+    stream = torch.cuda.current_stream()
+    # stand-alone latency of each frame (band DFT + beamformer), for p50 / p99
+    solo = []
+    for p, rf, im in zip(plans, rfs, imgs):
+        p.execute(rf, out=im, stream=stream)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        p.execute(rf, out=im, stream=stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        solo.append(a.elapsed_time(b))
+    batch = das.Batch(plans, rfs, imgs, n_streams=4)
+    for _ in range(args.warmup):
+        batch.execute(stream)
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    ev[0].record(stream)
+    for s in range(args.steps):
+        batch.execute(stream)
+        ev[s + 1].record(stream)
+    torch.cuda.synchronize()
+    done = batch.frame_times()                      # completion within the last batch
+    clk = clocks.stop()
+    total_ms = ev[0].elapsed_time(ev[-1])
+    n = len(plans)
+    terms = sum(p.info()["terms"] for p in plans)
+    out = {"metric": BATCH_METRIC, "value": n * args.steps / (total_ms * 1e-3), "unit": UNIT, "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32 (double-float phase)", "data": "synthetic",
+           "config": {"workload": "batch_%d_pw_frames_uneven_seed0" % n, "frames": n,
+                      "elements": sorted({p.n_elements for p in plans}), "angles": sorted({p.n_angles for p in plans}),
+                      "grid_sides": [min(p.n_x for p in plans), max(p.n_x for p in plans)], "n_streams": 4,
+                      "autotune": not args.no_autotune, "kernel_variants": variants,
+                      "l2": "a batch reads 1.5+ GB of RF and spectra, larger than L2", "rf_synthesis_s": synth_s},
+           "gterms_per_s": terms * args.steps / (total_ms * 1e-3) / 1e9,
+           "latency_ms": {"standalone_p50": float(np.percentile(solo, 50)),
+                          "standalone_p99": float(np.percentile(solo, 99)),
+                          "in_batch_completion_p50": float(np.percentile(done, 50)),
+                          "in_batch_completion_p99": float(np.percentile(done, 99)),
+                          "sum_of_standalone": float(np.sum(solo))},
+           "clocks": clk, "gpu_launches": args.steps * sum(1 + (1 if p.n_out == 1 else p.n_angles) for p in plans)}
+    print(json.dumps(out))
+    batch.close()
+    for p in plans:
+        p.close()
+
+
 def main():
     args = parse()
     import __graft_entry__ as g
     g.build()
-    if args.workload == "saft":
+    if args.workload == "batch":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the batch workload has no CPU arm; the CPU "
+                              "baseline of the headline is the cpwc workload"}))
+            return
+        run_batch(args)
+    elif args.workload == "saft":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the saft workload has no CPU arm; the CPU "
                               "baseline of the headline is the cpwc workload"}))
