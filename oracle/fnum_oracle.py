@@ -441,6 +441,62 @@ def _pw_core(px, pz, X, band, F, e_x, e_z, x_ref, window, norm, pitch, voxels):
 
 
 # ---------------------------------------------------------------------------
+# image-sharpness loss of a compounded plane-wave image and its gradients
+# (no counterpart in the reference; the forward model is das_pw_mex's)
+# ---------------------------------------------------------------------------
+def pw_sharpness_grad(positions_x, positions_z, rf, f_s, angles, element_width, element_pitch, c, f_bounds=None,
+                      index_t0=0.0, window=("boxcar", 0.0), F_number=None, normalization="on", c_freeze=None):
+    """FP64 loss L = -sum|I|^4 / (sum|I|^2)^2 of the compounded MEX-semantics image
+    I = sum over angles of das_pw_mex, with the DFT order, band, F table and
+    apertures frozen at c_freeze (default c) and the phases at c.
+    rf: [A, E, T].  Returns (L, dL/dc, dL/dX* as complex [E, K, A], image [Z, X]).
+    dL/dX* is the Wirtinger gradient: dL = 2 Re sum conj(dL/dX*) dX."""
+    px = np.asarray(positions_x, dtype=np.float64).ravel()
+    pz = np.asarray(positions_z, dtype=np.float64).ravel()
+    rf = np.asarray(rf, dtype=np.float64)
+    A, E, T = rf.shape
+    c0 = c if c_freeze is None else c_freeze
+    band = band_mex(pz, T, E, f_s, element_width, element_pitch, c0, f_bounds, index_t0)
+    F = _resolve_F(F_number, band, element_pitch, f_s, c0, default=("angle_lb", 70.0, 1.5, 10.0))
+    N, K = band.N_dft, band.K
+    ks = band.ks.astype(np.float64)
+    coef = 2.0 * math.pi * f_s / (N * c)               # rad per bin per metre at the trial c
+    X = np.stack([rf_band_spectra(rf[a].T, band) for a in range(A)], axis=2)   # [K, E, A]
+    norm = normalization != "off"
+    cache = []
+    image = np.zeros((pz.size, px.size), dtype=np.complex128)
+    for ix, x in enumerate(px):
+        a_w = _aperture_weights(window, x, pz, F, band, E, element_pitch)       # [K, Z, E]
+        W = a_w.sum(axis=2)
+        b = a_w / np.where(W == 0, 1.0, W)[..., None] if norm else a_w
+        b = np.where((W == 0)[..., None], 0.0, b)
+        d_rx = np.sqrt((band.ctr[None, :] - x) ** 2 + pz[:, None] ** 2)      # [Z, E]
+        ph, dph = [], []
+        for ia, th in enumerate(angles):
+            e_x, e_z = -math.sin(th), math.cos(th)
+            x_ref = -band.M * element_pitch if e_x >= 0 else band.M * element_pitch
+            d = (e_x * (x - x_ref) + e_z * pz)[:, None] + d_rx                 # [Z, E]
+            p = np.exp(1j * ks[:, None, None] * (coef * d[None] + band.add))    # [K, Z, E]
+            ph.append(p)
+            dph.append(p * (1j * ks[:, None, None] * (-coef * d[None] / c)))   # d(phase factor)/dc
+            image[:, ix] += (2.0 / N) * np.einsum("kze,kze,ke->z", b, p, X[:, :, ia])
+        cache.append((b, ph, dph))
+    m2 = np.abs(image) ** 2
+    S2, S4 = m2.sum(), (m2 * m2).sum()
+    L = -S4 / S2 ** 2
+    G = -2.0 * image * (m2 / S2 ** 2 - S4 / S2 ** 3)                            # dL/dI*
+    gX = np.zeros((K, E, A), dtype=np.complex128)
+    dLdc = 0.0
+    for ix in range(px.size):
+        b, ph, dph = cache[ix]
+        for ia in range(A):
+            gX[:, :, ia] += (2.0 / N) * np.einsum("z,kze,kze->ke", G[:, ix], b, np.conj(ph[ia]))
+            dI = (2.0 / N) * np.einsum("kze,kze,ke->z", b, dph[ia], X[:, :, ia])
+            dLdc += 2.0 * np.real(np.sum(np.conj(G[:, ix]) * dI))
+    return L, dLdc, np.transpose(gX, (1, 0, 2)), image
+
+
+# ---------------------------------------------------------------------------
 # das_pw, CPU (.m) semantics
 # ---------------------------------------------------------------------------
 
