@@ -17,7 +17,7 @@ EXPORTS = (
     "fnum_sa_plan_create", "fnum_plan_execute", "fnum_plan_execute_dft", "fnum_plan_execute_beamform",
     "fnum_plan_info_get", "fnum_plan_f_numbers", "fnum_plan_destroy", "fnum_diag_fp32_peak",
     "fnum_das_pw_noalloc", "fnum_bmode", "fnum_plan_autotune", "fnum_batch_create", "fnum_batch_execute",
-    "fnum_batch_frame_times", "fnum_batch_destroy",
+    "fnum_batch_frame_times", "fnum_batch_destroy", "fnum_pw_plan_set_sound_speed", "fnum_pw_sharpness_grad",
 )
 
 ABI_VERSION = 2   # FNUM_ABI_VERSION of include/fnum.h
@@ -172,6 +172,10 @@ def lib():
     L.fnum_batch_frame_times.argtypes = [C.c_void_p, _fp]
     L.fnum_batch_destroy.restype = C.c_int
     L.fnum_batch_destroy.argtypes = [C.c_void_p]
+    L.fnum_pw_plan_set_sound_speed.restype = C.c_int
+    L.fnum_pw_plan_set_sound_speed.argtypes = [C.c_void_p, C.c_double]
+    L.fnum_pw_sharpness_grad.restype = C.c_int
+    L.fnum_pw_sharpness_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_int, _dp, _dp, C.c_void_p, C.c_void_p]
     L.fnum_bmode.restype = C.c_int
     L.fnum_bmode.argtypes = [C.c_void_p, C.c_longlong, C.c_int, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
     if L.fnum_abi_version() != ABI_VERSION:

@@ -422,6 +422,16 @@ struct fnum_plan {
   std::vector<double> F, F2;
   fnum_plan_info info{};
   int nt = 0;
+  // plane wave: what the phase tables are built from (fnum_pw_plan_set_sound_speed)
+  std::vector<double> hx, hz, hang;
+  double fs = 0.0, pitch = 0.0, width = 0.0, t0 = 0.0, c = 0.0;
+  // sharpness-loss gradients (fnum_pw_sharpness_grad), allocated on first use
+  float2* adj_img = nullptr;
+  float* adj_invw = nullptr;
+  float2* adj_H = nullptr;
+  float2* adj_gX = nullptr;
+  double* adj_sums = nullptr;
+  bool adj_invw_ready = false;
 
   template <typename T>
   int alloc(T** p, size_t count) {
@@ -643,6 +653,14 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
     }
   }
   P->n_out = (flags & FNUM_FLAG_COMPOUND) ? 1 : na;
+  P->hx.assign(d->positions_x, d->positions_x + nx);
+  P->hz.assign(d->positions_z, d->positions_z + nz);
+  P->hang.assign(angles, angles + na);
+  P->fs = d->f_s;
+  P->pitch = d->element_pitch;
+  P->width = d->element_width;
+  P->t0 = d->index_t0;
+  P->c = d->c_0;
   P->info.N_dft = b.N; P->info.k_lb = b.k_lb; P->info.k_ub = b.k_ub; P->info.n_bins = b.K;
   P->info.n_x = nx; P->info.n_z = nz; P->info.n_elements = ne; P->info.n_angles = na; P->info.n_samples = d->n_samples;
   P->info.f_monotone = mono;
@@ -1249,6 +1267,81 @@ int fnum_batch_destroy(fnum_batch* batch) {
   if (!batch) return FNUM_OK;
   cudaSetDevice(batch->device);
   delete batch;
+  return FNUM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// sound speed and sharpness-loss gradients (no counterpart in the reference)
+// ---------------------------------------------------------------------------
+int fnum_pw_plan_set_sound_speed(fnum_plan* plan, double c_0) {
+  if (!plan || plan->kind != 0 || !(c_0 > 0.0) || !std::isfinite(c_0)) return FNUM_ERR_ARGUMENT;
+  FNUM_CUDA(cudaSetDevice(plan->device));
+  fnum::PWDev& D = plan->pw;
+  const Band& b = plan->band;
+  const double Ku = plan->fs / ((double)b.N * c_0);
+  GeomTables g;
+  build_geometry(plan->hx.data(), D.nx, plan->hz.data(), D.nz, D.ne, plan->width, plan->pitch, Ku, b.M, g);
+  const int na = D.na;
+  std::vector<dfl> ax((size_t)na * D.nx), az((size_t)na * D.nz);
+  for (int a = 0; a < na; ++a) {
+    const double ex = -sin(plan->hang[a]), ez = cos(plan->hang[a]);
+    const double xref = (ex >= 0) ? -b.M * plan->pitch : b.M * plan->pitch;
+    for (int i = 0; i < D.nx; ++i) ax[(size_t)a * D.nx + i] = to_df(Ku * ex * (plan->hx[i] - xref) + plan->t0 / b.N);
+    for (int j = 0; j < D.nz; ++j) az[(size_t)a * D.nz + j] = to_df(Ku * ez * plan->hz[j]);
+  }
+  FNUM_CUDA(cudaMemcpy((void*)D.col_u, g.col_u.data(), g.col_u.size() * sizeof(dfl), cudaMemcpyHostToDevice));
+  FNUM_CUDA(cudaMemcpy((void*)D.row_u2, g.row_u2.data(), g.row_u2.size() * sizeof(dfl), cudaMemcpyHostToDevice));
+  FNUM_CUDA(cudaMemcpy((void*)D.el_u, g.el_u.data(), g.el_u.size() * sizeof(dfl), cudaMemcpyHostToDevice));
+  FNUM_CUDA(cudaMemcpy((void*)D.tx_ax, ax.data(), ax.size() * sizeof(dfl), cudaMemcpyHostToDevice));
+  FNUM_CUDA(cudaMemcpy((void*)D.tx_az, az.data(), az.size() * sizeof(dfl), cudaMemcpyHostToDevice));
+  D.coef_f = (float)(2.0 * M_PI * plan->fs / ((double)b.N * c_0));
+  plan->c = c_0;
+  return FNUM_OK;
+}
+
+int fnum_pw_sharpness_grad(fnum_plan* plan, const void* d_rf, int rf_is_double, double* loss, double* dloss_dc,
+                           void* d_grad_spectra, void* stream) {
+  if (!plan || !d_rf || plan->kind != 0 || plan->n_out != 1) return FNUM_ERR_ARGUMENT;
+  FNUM_CUDA(cudaSetDevice(plan->device));
+  cudaStream_t st = (cudaStream_t)stream;
+  fnum::PWDev& D = plan->pw;
+  const long long nvox = (long long)D.nx * D.nz;
+  const size_t nspec = (size_t)D.ne * D.K * D.na;
+  int s = FNUM_OK;
+  if (!plan->adj_img) {
+    if ((s = plan->alloc(&plan->adj_img, (size_t)nvox)) || (s = plan->alloc(&plan->adj_invw, (size_t)nvox * D.K)) ||
+        (s = plan->alloc(&plan->adj_H, nspec)) || (s = plan->alloc(&plan->adj_gX, nspec)) ||
+        (s = plan->alloc(&plan->adj_sums, 4)))
+      return s;
+  }
+  if (!plan->adj_invw_ready) {
+    FNUM_CUDA(fnum::launch_pw_invw(D, plan->adj_invw, st));
+    plan->adj_invw_ready = true;
+  }
+  if ((s = plan_dft(plan, d_rf, rf_is_double, st))) return s;
+  if ((s = plan_beamform(plan, plan->adj_img, nullptr, nullptr, st))) return s;
+  FNUM_CUDA(fnum::launch_pw_sharp_sums(plan->adj_img, nvox, plan->adj_sums, st));
+  double S[2] = {0.0, 0.0};
+  FNUM_CUDA(cudaMemcpyAsync(S, plan->adj_sums, sizeof(S), cudaMemcpyDeviceToHost, st));
+  FNUM_CUDA(cudaStreamSynchronize(st));
+  float2* gX = d_grad_spectra ? (float2*)d_grad_spectra : plan->adj_gX;
+  if (!(S[0] > 0.0)) {  // an all-zero image: the loss is 0 and flat
+    FNUM_CUDA(cudaMemsetAsync(gX, 0, nspec * sizeof(float2), st));
+    FNUM_CUDA(cudaStreamSynchronize(st));
+    if (loss) *loss = 0.0;
+    if (dloss_dc) *dloss_dc = 0.0;
+    return FNUM_OK;
+  }
+  const double gs2 = 1.0 / (S[0] * S[0]), gs4 = S[1] / (S[0] * S[0] * S[0]);
+  FNUM_CUDA(fnum::launch_pw_adjoint(D, plan->adj_img, plan->adj_invw, (float)gs2, (float)gs4,
+                                    (float)(plan->t0 / plan->band.N), gX, plan->adj_H, st));
+  const double coef = 4.0 * M_PI * (2.0 / plan->band.N) / plan->c;
+  FNUM_CUDA(fnum::launch_pw_dldc(D, plan->adj_H, coef, plan->adj_sums + 2, st));
+  double g = 0.0;
+  FNUM_CUDA(cudaMemcpyAsync(&g, plan->adj_sums + 2, sizeof(double), cudaMemcpyDeviceToHost, st));
+  FNUM_CUDA(cudaStreamSynchronize(st));
+  if (loss) *loss = -S[1] / (S[0] * S[0]);
+  if (dloss_dc) *dloss_dc = g;
   return FNUM_OK;
 }
 

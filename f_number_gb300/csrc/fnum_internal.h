@@ -106,5 +106,11 @@ cudaError_t launch_pw_fused(const PWDev& d, int grid, float2* image, float* weig
 cudaError_t launch_pw_plain(const PWDev& d, float2* image, float* weights, cudaStream_t s);
 cudaError_t launch_sa_fused(const SADev& d, int grid, float2* image, float* wtx, float* wrx, cudaStream_t s);
 cudaError_t launch_sa_plain(const SADev& d, float2* image, float* wtx, float* wrx, cudaStream_t s);
+// sharpness-loss gradients of a compounded plane-wave plan (fnum_pw_sharpness_grad)
+cudaError_t launch_pw_invw(const PWDev& d, float* invw, cudaStream_t s);
+cudaError_t launch_pw_sharp_sums(const float2* img, long long n, double* sums, cudaStream_t s);
+cudaError_t launch_pw_adjoint(const PWDev& d, const float2* img, const float* invw, float gs2, float gs4, float t0N,
+                              float2* gX, float2* H, cudaStream_t s);
+cudaError_t launch_pw_dldc(const PWDev& d, const float2* H, double coef, double* out, cudaStream_t s);
 
 }  // namespace fnum

@@ -1320,3 +1320,221 @@ cudaError_t launch_sa_plain(const SADev& d, float2* image, float* wtx, float* wr
 }
 
 }  // namespace fnum
+
+namespace fnum {
+
+// ---------------------------------------------------------------------------
+// Gradients of an image-sharpness loss of the compounded plane-wave image
+//   L = -S4 / S2^2,  S2 = sum_v |I_v|^2,  S4 = sum_v |I_v|^4,
+// with the DFT order, band, F table and apertures frozen (only the phases
+// depend on the sound speed).  dL/dI_v* = G_v = -2 I_v (|I_v|^2/S2^2 - S4/S2^3).
+//   dL/dX*_{e,k,a} = (2/N) sum_v G_v b_{v,e,k} e^{-j 2 pi k u_{v,e,a}}
+//   dL/dc = 2 Re sum_{e,k,a} X (-j 2 pi k / c) (2/N) conj(H_{e,k,a}),
+//   H_{e,k,a} = sum_v G_v b_{v,e,k} e^{-j 2 pi k u} U_{v,e,a},  U = u - t0/N,
+// because u = f_s/(N c) (d_tx + d_rx) + t0/N gives du/dc = -U/c.
+// No counterpart in the reference.
+// ---------------------------------------------------------------------------
+
+// 1/W (or 1, or 0 for an empty aperture) per voxel and band bin: [voxel][K]
+template <int WIN>
+__global__ void __launch_bounds__(NTHREADS) pw_invw_kernel(const PWDev d, float* __restrict__ invw) {
+  const long long v = (long long)blockIdx.x * NTHREADS + threadIdx.x;
+  if (v >= (long long)d.nx * d.nz) return;
+  const int i = (int)(v / d.nz), j = (int)(v - (long long)i * d.nz);
+  const dfl xp = d.col_p[i], zp = d.row_p[j], xm = d.col_m[i];
+  const int emid = d.col_emid[i];
+  const float inv_par = (d.window_par > 0.0f) ? 1.0f / d.window_par : 0.0f;
+  int prev = -1;
+  float iw = 0.0f;
+  for (int kk = 0; kk < d.K; ++kk) {
+    int ilb, iub;
+    aperture(xp, zp, d.g[kk], d.ne, ilb, iub);
+    const int code = seg_code(ilb, iub);
+    if (code != prev) {
+      const float Ll = half_left(d.el_lb, xm, ilb, d.ne), Lr = half_right(d.el_ub, xm, iub);
+      const float W = aperture_sum_closed<WIN>(d, inv_par, xm, emid, ilb, iub, (Ll > 0.0f) ? 1.0f / Ll : 0.0f,
+                                               (Lr > 0.0f) ? 1.0f / Lr : 0.0f);
+      iw = (W > 0.0f) ? (d.norm ? 1.0f / W : 1.0f) : 0.0f;
+      prev = code;
+    }
+    invw[(size_t)v * d.K + kk] = iw;
+  }
+}
+
+// S2, S4 of an image (double accumulation)
+__global__ void __launch_bounds__(256) pw_sharp_sums_kernel(const float2* __restrict__ img, long long n,
+                                                            double* __restrict__ sums) {
+  __shared__ double r2[8], r4[8];
+  double s2 = 0.0, s4 = 0.0;
+  for (long long i = (long long)blockIdx.x * 256 + threadIdx.x; i < n; i += (long long)gridDim.x * 256) {
+    const float2 v = img[i];
+    const double m2 = (double)v.x * v.x + (double)v.y * v.y;
+    s2 += m2;
+    s4 += m2 * m2;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    s4 += __shfl_xor_sync(0xffffffffu, s4, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    r2[threadIdx.x >> 5] = s2;
+    r4[threadIdx.x >> 5] = s4;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < 8; ++w) {
+      a += r2[w];
+      b += r4[w];
+    }
+    atomicAdd(&sums[0], a);
+    atomicAdd(&sums[1], b);
+  }
+}
+
+// One thread per (element e, band bin k), NA angles per pass: sums over every
+// voxel whose aperture holds e at k.  Phases are exact per term (cis_ku);
+// each column's terms are summed in FP32 and the columns in FP64.
+constexpr int ADJ_NA = 6;
+template <int WIN>
+__global__ void __launch_bounds__(128)
+pw_adjoint_kernel(const PWDev d, const float2* __restrict__ img, const float* __restrict__ invw, float gs2, float gs4,
+                  float t0N, float2* __restrict__ gX, float2* __restrict__ H) {
+  const int t = blockIdx.x * 128 + threadIdx.x;
+  if (t >= d.ne * d.K) return;
+  const int e = t / d.K, kk = t - e * d.K, k = d.k_lb + kk;
+  const dfl g = d.g[kk];
+  const dfl cm = d.el_m[e], cu = d.el_u[e];
+  const float inv_par = (d.window_par > 0.0f) ? 1.0f / d.window_par : 0.0f;
+  for (int a0 = 0; a0 < d.na; a0 += ADJ_NA) {
+    double sXr[ADJ_NA], sXi[ADJ_NA], sHr[ADJ_NA], sHi[ADJ_NA];
+#pragma unroll
+    for (int q = 0; q < ADJ_NA; ++q) sXr[q] = sXi[q] = sHr[q] = sHi[q] = 0.0;
+    for (int i = 0; i < d.nx; ++i) {
+      const dfl xm = d.col_m[i], xp = d.col_p[i];
+      const bool left = e < d.col_emid[i];
+      const float dxa = fabsf((cm.x - xm.x) + (cm.y - xm.y));
+      const dfl du2 = df_sqr(df_sub(cu, d.col_u[i]));
+      float pXr[ADJ_NA], pXi[ADJ_NA], pHr[ADJ_NA], pHi[ADJ_NA];
+#pragma unroll
+      for (int q = 0; q < ADJ_NA; ++q) pXr[q] = pXi[q] = pHr[q] = pHi[q] = 0.0f;
+      bool any = false;
+      for (int j = 0; j < d.nz; ++j) {
+        int ilb, iub;
+        aperture(xp, d.row_p[j], g, d.ne, ilb, iub);
+        if (left ? (e < ilb) : (e > iub)) continue;
+        const float iw = invw[((size_t)i * d.nz + j) * d.K + kk];
+        if (iw == 0.0f) continue;
+        float L;
+        if (left) {
+          const dfl l = d.el_lb[ilb];
+          L = (xm.x - l.x) + (xm.y - l.y);
+        } else {
+          const dfl u = d.el_ub[iub];
+          L = (u.x - xm.x) + (u.y - xm.y);
+        }
+        const float b = win_t<WIN>(d.window_par, inv_par, dxa / L) * iw;
+        if (b == 0.0f) continue;
+        any = true;
+        const float2 I = img[(size_t)i * d.nz + j];
+        const float m2 = I.x * I.x + I.y * I.y;
+        const float cg = -2.0f * (m2 * gs2 - gs4) * b;
+        const float Gr = cg * I.x, Gi = cg * I.y;
+        const dfl urx = df_sqrt(df_add(du2, d.row_u2[j]));
+#pragma unroll
+        for (int q = 0; q < ADJ_NA; ++q) {
+          const int aa = a0 + q;
+          if (aa < d.na) {
+            const dfl u = df_add(urx, df_add(d.tx_ax[(size_t)aa * d.nx + i], d.tx_az[(size_t)aa * d.nz + j]));
+            const float2 ph = cis_ku(k, u);
+            const float Tr = fmaf(Gr, ph.x, Gi * ph.y), Ti = fmaf(Gi, ph.x, -Gr * ph.y);  // G conj(ph)
+            const float U = (u.x - t0N) + u.y;
+            pXr[q] += Tr;
+            pXi[q] += Ti;
+            pHr[q] = fmaf(Tr, U, pHr[q]);
+            pHi[q] = fmaf(Ti, U, pHi[q]);
+          }
+        }
+      }
+      if (any) {
+#pragma unroll
+        for (int q = 0; q < ADJ_NA; ++q) {
+          sXr[q] += pXr[q];
+          sXi[q] += pXi[q];
+          sHr[q] += pHr[q];
+          sHi[q] += pHi[q];
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < ADJ_NA; ++q) {
+      const int aa = a0 + q;
+      if (aa < d.na) {
+        const size_t o = ((size_t)e * d.K + kk) * d.na + aa;
+        gX[o] = make_float2((float)(d.scale * sXr[q]), (float)(d.scale * sXi[q]));
+        H[o] = make_float2((float)sHr[q], (float)sHi[q]);
+      }
+    }
+  }
+}
+
+// dL/dc = sum_{e,k,a} coef k Im(X conj(H)),  coef = 4 pi (2/N) / c
+__global__ void __launch_bounds__(256) pw_dldc_kernel(const PWDev d, const float2* __restrict__ H, double coef,
+                                                      double* __restrict__ out) {
+  __shared__ double r[8];
+  double s = 0.0;
+  const long long n = (long long)d.ne * d.K * d.na;
+  for (long long i = (long long)blockIdx.x * 256 + threadIdx.x; i < n; i += (long long)gridDim.x * 256) {
+    const int kk = (int)((i / d.na) % d.K);
+    const float2 x = d.X[i], h = H[i];
+    s += (double)(d.k_lb + kk) * ((double)x.y * h.x - (double)x.x * h.y);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) r[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0;
+    for (int w = 0; w < 8; ++w) a += r[w];
+    atomicAdd(out, coef * a);
+  }
+}
+
+cudaError_t launch_pw_invw(const PWDev& d, float* invw, cudaStream_t s) {
+  const long long nv = (long long)d.nx * d.nz;
+  const int grid = (int)((nv + NTHREADS - 1) / NTHREADS);
+  switch (d.window_id) {
+    case 0: pw_invw_kernel<0><<<grid, NTHREADS, 0, s>>>(d, invw); break;
+    case 1: pw_invw_kernel<1><<<grid, NTHREADS, 0, s>>>(d, invw); break;
+    case 2: pw_invw_kernel<2><<<grid, NTHREADS, 0, s>>>(d, invw); break;
+    default: pw_invw_kernel<4><<<grid, NTHREADS, 0, s>>>(d, invw); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pw_sharp_sums(const float2* img, long long n, double* sums, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(sums, 0, 2 * sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  pw_sharp_sums_kernel<<<1216, 256, 0, s>>>(img, n, sums);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pw_adjoint(const PWDev& d, const float2* img, const float* invw, float gs2, float gs4, float t0N,
+                              float2* gX, float2* H, cudaStream_t s) {
+  const int grid = (d.ne * d.K + 127) / 128;
+  switch (d.window_id) {
+    case 0: pw_adjoint_kernel<0><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, gX, H); break;
+    case 1: pw_adjoint_kernel<1><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, gX, H); break;
+    case 2: pw_adjoint_kernel<2><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, gX, H); break;
+    default: pw_adjoint_kernel<4><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, gX, H); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pw_dldc(const PWDev& d, const float2* H, double coef, double* out, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  pw_dldc_kernel<<<608, 256, 0, s>>>(d, H, coef, out);
+  return cudaGetLastError();
+}
+
+}  // namespace fnum

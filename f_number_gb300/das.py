@@ -489,6 +489,33 @@ class PWPlan(_Plan):
         self.n_out = 1 if compound else self._angles.size
 
 
+def _pw_set_sound_speed(self, c_0):
+    """Re-times the phase tables at sound speed c_0 (fnum_pw_plan_set_sound_speed);
+    DFT order, band, F table and apertures stay those of the creation speed."""
+    _lib.check(_lib.lib().fnum_pw_plan_set_sound_speed(self._ptr, float(c_0)))
+
+
+def _pw_sharpness_grad(self, rf, grad_spectra=True, stream=None):
+    """Sharpness loss L = -sum|I|^4 / (sum|I|^2)^2 of the compounded image of rf,
+    dL/dc, and (optionally) the Wirtinger gradient dL/dX* of the band spectra as
+    a complex64 CUDA tensor [n_elements, n_bins, n_angles]
+    (fnum_pw_sharpness_grad).  Returns (L, dL/dc, gradient or None)."""
+    import torch
+    g = None
+    if grad_spectra:
+        g = torch.empty((self.n_elements, self.n_bins, self.n_angles), dtype=torch.complex64, device=rf.device)
+    L = _lib.C.c_double(0.0)
+    dc = _lib.C.c_double(0.0)
+    _lib.check(_lib.lib().fnum_pw_sharpness_grad(self._ptr, rf.data_ptr(), int(rf.dtype == torch.float64),
+                                                 _lib.C.byref(L), _lib.C.byref(dc),
+                                                 g.data_ptr() if g is not None else None, self._stream_ptr(stream)))
+    return L.value, dc.value, g
+
+
+PWPlan.set_sound_speed = _pw_set_sound_speed
+PWPlan.sharpness_grad = _pw_sharpness_grad
+
+
 class SAPlan(_Plan):
     """Synthetic-aperture plan."""
     _saft = True

@@ -258,6 +258,22 @@ int fnum_batch_execute(fnum_batch* batch, void* stream);
 int fnum_batch_frame_times(const fnum_batch* batch, float* ms);
 int fnum_batch_destroy(fnum_batch* batch);
 
+/* --- image-sharpness gradients (no counterpart in the reference) --------- */
+/* Re-times a plane-wave plan's phase tables at sound speed c_0.  The DFT
+   order, band, F table and apertures stay those of the speed the plan was
+   created with, so images at nearby speeds differ only in their phases. */
+int fnum_pw_plan_set_sound_speed(fnum_plan* plan, double c_0);
+/* For a compounded plane-wave plan (FNUM_FLAG_COMPOUND): beamforms d_rf and
+   returns the sharpness loss L = -sum|I|^4 / (sum|I|^2)^2 of the image,
+   dL/dc at the plan's current sound speed (band, F table and apertures held
+   fixed), and, if d_grad_spectra is not NULL, the Wirtinger gradient dL/dX*
+   of the band spectra (device float2 [n_elements][n_bins][n_angles]; a change
+   dX of the spectra changes L by 2 Re sum conj(dL/dX*) dX).  The first call
+   allocates the plan's gradient buffers (a 1/W table of n_x n_z n_bins floats
+   among them).  Synchronises `stream`. */
+int fnum_pw_sharpness_grad(fnum_plan* plan, const void* d_rf, int rf_is_double, double* loss, double* dloss_dc,
+                           void* d_grad_spectra, void* stream);
+
 /* copies the plan's F table (n_bins values; two tables for SA: tx then rx) */
 int fnum_plan_f_numbers(const fnum_plan* plan, double* values);
 int fnum_plan_destroy(fnum_plan* plan);

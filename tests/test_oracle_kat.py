@@ -219,3 +219,29 @@ def test_saft_normalisation_semantics():
     assert np.abs(off_off).max() > 0
     on_on, wt, wr, _ = O.das_sa_mex(px, pz, data, *args, "on", "on")
     assert np.all(wt > 0) and np.all(wr > 0)
+
+
+def test_sharpness_gradient_oracle_matches_finite_differences():
+    """The FP64 gradients of the sharpness loss (oracle.pw_sharpness_grad) against
+    central differences: h = 1e-3 m/s on c (band, F table and apertures frozen)
+    and a random RF direction (dL = 2 Re sum conj(dL/dX*) dX)."""
+    from f_number_gb300 import synth
+    rng = np.random.default_rng(3)
+    arr = synth.LinearArray(16, 0.3048e-3, 0.918 * 0.3048e-3)
+    angles = [-0.05, 0.05]
+    px, pz = np.linspace(-2e-3, 2e-3, 6), np.linspace(5e-3, 9e-3, 7)
+    rf = synth.pw_rf(rng, arr, synth.random_points(rng, 3, (-2e-3, 2e-3), (5e-3, 9e-3)), angles, 384, 20e6, 1540.0)
+    F = {"kind": "grating.angle_lb", "angle_lb_deg": 60.0, "F_number_ub": 1.5, "distance_deg": 10.0}
+    kw = dict(f_bounds=(2e6, 7e6), index_t0=0.0, window=("hann", 0.0), F_number=F, normalization="on")
+    run = lambda r, c: O.pw_sharpness_grad(px, pz, r, 20e6, angles, arr.width, arr.pitch, c, c_freeze=1540.0, **kw)
+    L, dLdc, gX, _ = run(rf, 1540.0)
+    h = 1e-3
+    fd = (run(rf, 1540.0 + h)[0] - run(rf, 1540.0 - h)[0]) / (2 * h)
+    assert abs(fd - dLdc) <= 1e-6 * abs(dLdc)
+    d_rf = rng.standard_normal(rf.shape)
+    band = O.band_mex(pz, 384, 16, 20e6, arr.width, arr.pitch, 1540.0, (2e6, 7e6), 0.0)
+    dX = np.stack([O.rf_band_spectra(d_rf[a].T, band) for a in range(2)], axis=2).transpose(1, 0, 2)
+    an = 2 * np.real(np.sum(np.conj(gX) * dX))
+    eps = 1e-5                                 # relative to the RF's ~0.13 rms (central differences, error ~eps^2)
+    fd = (run(rf + eps * d_rf, 1540.0)[0] - run(rf - eps * d_rf, 1540.0)[0]) / (2 * eps)
+    assert abs(fd - an) <= 1e-6 * abs(an)
