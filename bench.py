@@ -43,10 +43,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--grid", type=int, default=512, help="voxels per side (512 = the benchmark grid; smaller "
                     "sizes keep the same 0.06 mm spacing, for profiling)")
-    ap.add_argument("--workload", default="cpwc", choices=["cpwc", "saft", "batch"],
+    ap.add_argument("--workload", default="cpwc", choices=["cpwc", "saft", "batch", "adjoint"],
                     help="cpwc (default, the headline); saft: 128 x 128 synthetic aperture, 3072 samples at "
                     "40 MHz, 400 x 400 voxels, directivity F-number, boxcar windows; batch: 64 plane-wave frames "
-                    "of uneven shape in one CUDA graph")
+                    "of uneven shape in one CUDA graph; adjoint: sharpness-loss gradients (dL/dc, dL/dX*) of the cpwc "
+                    "geometry with RF simulated at 1500 m/s")
     ap.add_argument("--frames", type=int, default=64, help="batch: frames per batch")
     ap.add_argument("--no-autotune", action="store_true", help="batch: keep each plan's default kernel variant")
     ap.add_argument("--band", default="full", choices=["full", "2-7"],
@@ -452,10 +453,72 @@ def run_batch(args):
         p.close()
 
 
+# ---------------------------------------------------------------------------
+# adjoint workload: sharpness-loss gradients of the CPWC frame
+# ---------------------------------------------------------------------------
+ADJ_METRIC = "sharpness-gradient evaluations/s (CPWC 11 angles, 512x512: loss, dL/dc, dL/dX*)"
+
+
+def run_adjoint(args):
+    import torch
+    from f_number_gb300 import das, synth
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    wl, win, fn = workload(args.grid)
+    # echoes simulated at 1500 m/s, beamformed at trial speeds (band, F table, apertures frozen at 1540)
+    rng = np.random.default_rng(1)
+    xr, zr = (-15e-3, 15e-3), (5e-3, 45e-3)
+    sc = synth.merge(synth.random_points(rng, 100, xr, zr), synth.speckle_with_cyst(rng, 2000, xr, zr, (0.0, 20e-3),
+                                                                                      5e-3))
+    rf = torch.tensor(synth.pw_rf(rng, wl.array, sc, wl.angles, wl.n_samples, wl.f_s, 1500.0, snr_db=30.0),
+                      dtype=torch.float32, device=dev)
+    plan = das.PWPlan(wl.positions_x, wl.positions_z, wl.n_samples, wl.array.n_elements, wl.f_s, wl.angles,
+                      wl.array.width, wl.array.pitch, wl.c, list(wl.f_bounds), 0.0, win, fn, device=0, compound=True)
+    sweep = {}
+    for c in (1450.0, 1500.0, 1550.0):
+        plan.set_sound_speed(c)
+        L, dc, _ = plan.sharpness_grad(rf, grad_spectra=False)
+        sweep["%g" % c] = {"loss": L, "dL_dc": dc}
+    plan.set_sound_speed(1500.0)
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        plan.sharpness_grad(rf, stream=stream)
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        plan.sharpness_grad(rf, stream=stream)          # synchronises: loss and dL/dc reach the host
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    clk = clocks.stop()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    img = torch.empty((1, plan.n_x, plan.n_z), dtype=torch.complex64, device=dev)
+    a.record(stream)
+    plan.execute(rf, out=img, stream=stream)
+    b.record(stream)
+    torch.cuda.synchronize()
+    out = {"metric": ADJ_METRIC, "value": args.steps / dt, "unit": "evaluations/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32 (double-float phase, FP64 reductions)", "data": "synthetic",
+           "config": {"workload": "adjoint_cpwc_11angles_128el_2048smp_%dx%d_rf_at_1500" % (args.grid, args.grid),
+                      "trial_c": 1500.0, "frozen_at_c": 1540.0},
+           "forward_ms": a.elapsed_time(b), "sweep": sweep, "clocks": clk}
+    print(json.dumps(out))
+    plan.close()
+
+
 def main():
     args = parse()
     import __graft_entry__ as g
     g.build()
+    if args.workload == "adjoint":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no adjoint"}))
+            return
+        run_adjoint(args)
+        return
     if args.workload == "batch":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the batch workload has no CPU arm; the CPU "
