@@ -1392,87 +1392,124 @@ __global__ void __launch_bounds__(256) pw_sharp_sums_kernel(const float2* __rest
   }
 }
 
-// One thread per (element e, band bin k), NA angles per pass: sums over every
-// voxel whose aperture holds e at k.  Phases are exact per term (cis_ku);
-// each column's terms are summed in FP32 and the columns in FP64.
-constexpr int ADJ_NA = 6;
+// One block per band bin k, one thread per element (elements beyond the block
+// size run as further passes), ADJ_NA angles per pass.  Voxels are taken in
+// batches of ADJ_VB: the block first stages, per voxel, what every element
+// shares -- the transmit phasors e^{j 2 pi k u_tx} of the pass's angles, the
+// aperture at bin k, 1/W and G -- then each thread adds its element's terms:
+// one exact receive phasor e^{j 2 pi k u_rx} per (voxel, element) times the
+// staged transmit phasors.  Each batch is summed in FP32 and added in FP64.
+constexpr int ADJ_NA = 11;
+constexpr int ADJ_VB = 32;
 template <int WIN>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 2)
 pw_adjoint_kernel(const PWDev d, const float2* __restrict__ img, const float* __restrict__ invw, float gs2, float gs4,
                   float t0N, float2* __restrict__ gX, float2* __restrict__ H) {
-  const int t = blockIdx.x * 128 + threadIdx.x;
-  if (t >= d.ne * d.K) return;
-  const int e = t / d.K, kk = t - e * d.K, k = d.k_lb + kk;
+  __shared__ float2 sT[ADJ_VB][ADJ_NA];   // transmit phasor
+  __shared__ float sUt[ADJ_VB][ADJ_NA];   // u_tx - t0/N
+  __shared__ float2 sG[ADJ_VB];           // G_v / W_{v,k} (0: no contribution)
+  __shared__ int sAp[ADJ_VB][3];          // i_lb, i_ub, first element right of x
+  __shared__ int sCol[ADJ_VB], sRow[ADJ_VB];
+  const int tid = threadIdx.x;
+  const int kk = blockIdx.x, k = d.k_lb + kk;
   const dfl g = d.g[kk];
-  const dfl cm = d.el_m[e], cu = d.el_u[e];
+  const long long nvox = (long long)d.nx * d.nz;
   const float inv_par = (d.window_par > 0.0f) ? 1.0f / d.window_par : 0.0f;
-  for (int a0 = 0; a0 < d.na; a0 += ADJ_NA) {
-    double sXr[ADJ_NA], sXi[ADJ_NA], sHr[ADJ_NA], sHi[ADJ_NA];
+  for (int e0 = 0; e0 < d.ne; e0 += 128) {
+    const int e = e0 + tid;
+    const bool has_e = e < d.ne;
+    const int ec = min(e, d.ne - 1);
+    const dfl cm = d.el_m[ec], cu = d.el_u[ec];
+    for (int a0 = 0; a0 < d.na; a0 += ADJ_NA) {
+      const int nag = min(ADJ_NA, d.na - a0);
+      double sXr[ADJ_NA], sXi[ADJ_NA], sHr[ADJ_NA], sHi[ADJ_NA];
 #pragma unroll
-    for (int q = 0; q < ADJ_NA; ++q) sXr[q] = sXi[q] = sHr[q] = sHi[q] = 0.0;
-    for (int i = 0; i < d.nx; ++i) {
-      const dfl xm = d.col_m[i], xp = d.col_p[i];
-      const bool left = e < d.col_emid[i];
-      const float dxa = fabsf((cm.x - xm.x) + (cm.y - xm.y));
-      const dfl du2 = df_sqr(df_sub(cu, d.col_u[i]));
-      float pXr[ADJ_NA], pXi[ADJ_NA], pHr[ADJ_NA], pHi[ADJ_NA];
-#pragma unroll
-      for (int q = 0; q < ADJ_NA; ++q) pXr[q] = pXi[q] = pHr[q] = pHi[q] = 0.0f;
-      bool any = false;
-      for (int j = 0; j < d.nz; ++j) {
-        int ilb, iub;
-        aperture(xp, d.row_p[j], g, d.ne, ilb, iub);
-        if (left ? (e < ilb) : (e > iub)) continue;
-        const float iw = invw[((size_t)i * d.nz + j) * d.K + kk];
-        if (iw == 0.0f) continue;
-        float L;
-        if (left) {
-          const dfl l = d.el_lb[ilb];
-          L = (xm.x - l.x) + (xm.y - l.y);
-        } else {
-          const dfl u = d.el_ub[iub];
-          L = (u.x - xm.x) + (u.y - xm.y);
+      for (int q = 0; q < ADJ_NA; ++q) sXr[q] = sXi[q] = sHr[q] = sHi[q] = 0.0;
+      for (long long v0 = 0; v0 < nvox; v0 += ADJ_VB) {
+        const int nvb = (int)min((long long)ADJ_VB, nvox - v0);
+        __syncthreads();  // the previous batch is consumed
+        for (int q = tid; q < nvb; q += 128) {
+          const long long v = v0 + q;
+          const int i = (int)(v / d.nz), j = (int)(v - (long long)i * d.nz);
+          int ilb, iub;
+          aperture(d.col_p[i], d.row_p[j], g, d.ne, ilb, iub);
+          const float iw = invw[(size_t)v * d.K + kk];
+          const float2 I = img[v];
+          const float cg = -2.0f * ((I.x * I.x + I.y * I.y) * gs2 - gs4) * iw;
+          sG[q] = make_float2(cg * I.x, cg * I.y);
+          sAp[q][0] = ilb;
+          sAp[q][1] = iub;
+          sAp[q][2] = d.col_emid[i];
+          sCol[q] = i;
+          sRow[q] = j;
         }
-        const float b = win_t<WIN>(d.window_par, inv_par, dxa / L) * iw;
-        if (b == 0.0f) continue;
-        any = true;
-        const float2 I = img[(size_t)i * d.nz + j];
-        const float m2 = I.x * I.x + I.y * I.y;
-        const float cg = -2.0f * (m2 * gs2 - gs4) * b;
-        const float Gr = cg * I.x, Gi = cg * I.y;
-        const dfl urx = df_sqrt(df_add(du2, d.row_u2[j]));
+        for (int q = tid; q < nvb * nag; q += 128) {
+          const int vb = q / nag, a = q - vb * nag, aa = a0 + a;
+          const long long v = v0 + vb;
+          const int i = (int)(v / d.nz), j = (int)(v - (long long)i * d.nz);
+          const dfl ut = df_add(d.tx_ax[(size_t)aa * d.nx + i], d.tx_az[(size_t)aa * d.nz + j]);
+          sT[vb][a] = cis_ku(k, ut);
+          sUt[vb][a] = (ut.x - t0N) + ut.y;
+        }
+        __syncthreads();
+        if (!has_e) continue;
+        float pXr[ADJ_NA], pXi[ADJ_NA], pHr[ADJ_NA], pHi[ADJ_NA];
 #pragma unroll
-        for (int q = 0; q < ADJ_NA; ++q) {
-          const int aa = a0 + q;
-          if (aa < d.na) {
-            const dfl u = df_add(urx, df_add(d.tx_ax[(size_t)aa * d.nx + i], d.tx_az[(size_t)aa * d.nz + j]));
-            const float2 ph = cis_ku(k, u);
-            const float Tr = fmaf(Gr, ph.x, Gi * ph.y), Ti = fmaf(Gi, ph.x, -Gr * ph.y);  // G conj(ph)
-            const float U = (u.x - t0N) + u.y;
-            pXr[q] += Tr;
-            pXi[q] += Ti;
-            pHr[q] = fmaf(Tr, U, pHr[q]);
-            pHi[q] = fmaf(Ti, U, pHi[q]);
+        for (int q = 0; q < ADJ_NA; ++q) pXr[q] = pXi[q] = pHr[q] = pHi[q] = 0.0f;
+        for (int vb = 0; vb < nvb; ++vb) {
+          const float2 G = sG[vb];
+          if (G.x == 0.0f && G.y == 0.0f) continue;
+          const int ilb = sAp[vb][0], iub = sAp[vb][1];
+          const bool left = e < sAp[vb][2];
+          if (left ? (e < ilb) : (e > iub)) continue;
+          const int i = sCol[vb], j = sRow[vb];
+          const dfl xm = d.col_m[i];
+          float L;
+          if (left) {
+            const dfl l = d.el_lb[ilb];
+            L = (xm.x - l.x) + (xm.y - l.y);
+          } else {
+            const dfl u = d.el_ub[iub];
+            L = (u.x - xm.x) + (u.y - xm.y);
+          }
+          const float b = win_t<WIN>(d.window_par, inv_par, fabsf((cm.x - xm.x) + (cm.y - xm.y)) / L);
+          if (b == 0.0f) continue;
+          const float Gr = G.x * b, Gi = G.y * b;
+          const dfl urx = df_sqrt(df_add(df_sqr(df_sub(cu, d.col_u[i])), d.row_u2[j]));
+          const float2 P = cis_ku(k, urx);
+          const float ur = urx.x + urx.y;
+          // term = G b conj(P T) = (G b conj(P)) conj(T)
+          const float Qr = fmaf(Gr, P.x, Gi * P.y), Qi = fmaf(Gi, P.x, -Gr * P.y);
+#pragma unroll
+          for (int a = 0; a < ADJ_NA; ++a) {
+            if (a < nag) {
+              const float2 T = sT[vb][a];
+              const float Tr = fmaf(Qr, T.x, Qi * T.y), Ti = fmaf(Qi, T.x, -Qr * T.y);
+              const float U = ur + sUt[vb][a];
+              pXr[a] += Tr;
+              pXi[a] += Ti;
+              pHr[a] = fmaf(Tr, U, pHr[a]);
+              pHi[a] = fmaf(Ti, U, pHi[a]);
+            }
           }
         }
-      }
-      if (any) {
 #pragma unroll
-        for (int q = 0; q < ADJ_NA; ++q) {
-          sXr[q] += pXr[q];
-          sXi[q] += pXi[q];
-          sHr[q] += pHr[q];
-          sHi[q] += pHi[q];
+        for (int a = 0; a < ADJ_NA; ++a) {
+          sXr[a] += pXr[a];
+          sXi[a] += pXi[a];
+          sHr[a] += pHr[a];
+          sHi[a] += pHi[a];
         }
       }
-    }
+      if (has_e) {
 #pragma unroll
-    for (int q = 0; q < ADJ_NA; ++q) {
-      const int aa = a0 + q;
-      if (aa < d.na) {
-        const size_t o = ((size_t)e * d.K + kk) * d.na + aa;
-        gX[o] = make_float2((float)(d.scale * sXr[q]), (float)(d.scale * sXi[q]));
-        H[o] = make_float2((float)sHr[q], (float)sHi[q]);
+        for (int a = 0; a < ADJ_NA; ++a) {
+          if (a < nag) {
+            const size_t o = ((size_t)e * d.K + kk) * d.na + a0 + a;
+            gX[o] = make_float2((float)(d.scale * sXr[a]), (float)(d.scale * sXi[a]));
+            H[o] = make_float2((float)sHr[a], (float)sHi[a]);
+          }
+        }
       }
     }
   }
@@ -1520,7 +1557,7 @@ cudaError_t launch_pw_sharp_sums(const float2* img, long long n, double* sums, c
 
 cudaError_t launch_pw_adjoint(const PWDev& d, const float2* img, const float* invw, float gs2, float gs4, float t0N,
                               float2* gX, float2* H, cudaStream_t s) {
-  const int grid = (d.ne * d.K + 127) / 128;
+  const int grid = d.K;
   switch (d.window_id) {
     case 0: pw_adjoint_kernel<0><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, gX, H); break;
     case 1: pw_adjoint_kernel<1><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, gX, H); break;
