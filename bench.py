@@ -308,15 +308,17 @@ def run_ours(args):
 SA_METRIC = "SAFT frames/s (128 tx x 128 rx, 3072 smp, 400x400)"
 
 
-def saft_workload(band):
+def saft_workload(band, grid=400):
     from f_number_gb300 import synth
-    return synth.saft_128(seed=0, f_bounds=None if band == "full" else (2e6, 7e6))
+    return synth.saft_128(seed=0, grid=(grid, grid), f_bounds=None if band == "full" else (2e6, 7e6))
 
 
 def saft_config(wl, kernel, band):
-    return {"workload": "saft_128x128_3072smp_40MHz_400x400_%s_boxcar_perrot" % ("fullband" if band == "full"
-                                                                                   else "2-7MHz"),
-            "n_elements": wl.array.n_elements, "n_samples": wl.n_samples, "grid": [400, 400], "kernel": kernel,
+    g = "%dx%d" % (wl.positions_x.size, wl.positions_z.size)
+    return {"workload": "saft_128x128_3072smp_40MHz_%s_%s_boxcar_perrot" % (g, "fullband" if band == "full"
+                                                                          else "2-7MHz"),
+            "n_elements": wl.array.n_elements, "n_samples": wl.n_samples,
+            "grid": [int(wl.positions_x.size), int(wl.positions_z.size)], "kernel": kernel,
             "l2": "inputs larger than L2 (201 MB RF, band spectra up to 261 MB)", "data": "synthetic seeded RF"}
 
 
@@ -327,7 +329,7 @@ def run_saft(args):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    wl = saft_workload(args.band)
+    wl = saft_workload(args.band, 400 if args.grid == 512 else args.grid)
     fn = f_numbers.directivity.perrot(0.918)
     plan = das.SAPlan(wl.positions_x, wl.positions_z, wl.n_samples, wl.array.n_elements, wl.f_s, wl.array.width,
                       wl.array.pitch, wl.c, wl.f_bounds, 0.0, windows.boxcar(), windows.boxcar(), fn, fn,
