@@ -1400,7 +1400,7 @@ __global__ void __launch_bounds__(256) pw_sharp_sums_kernel(const float2* __rest
 // one exact receive phasor e^{j 2 pi k u_rx} per (voxel, element) times the
 // staged transmit phasors.  Each batch is summed in FP32 and added in FP64.
 constexpr int ADJ_NA = 11;
-constexpr int ADJ_VB = 32;
+constexpr int ADJ_VB = 128;
 template <int WIN>
 __global__ void __launch_bounds__(128, 2)
 pw_adjoint_kernel(const PWDev d, const float2* __restrict__ img, const float* __restrict__ invw, float gs2, float gs4,
