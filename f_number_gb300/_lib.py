@@ -18,22 +18,24 @@ EXPORTS = (
     "fnum_plan_info_get", "fnum_plan_f_numbers", "fnum_plan_destroy", "fnum_diag_fp32_peak",
     "fnum_das_pw_noalloc", "fnum_bmode", "fnum_plan_autotune", "fnum_batch_create", "fnum_batch_execute",
     "fnum_batch_frame_times", "fnum_batch_destroy", "fnum_pw_plan_set_sound_speed", "fnum_pw_sharpness_grad",
+    "fnum_plan_m_signal",
 )
 
-ABI_VERSION = 2   # FNUM_ABI_VERSION of include/fnum.h
+ABI_VERSION = 3   # FNUM_ABI_VERSION of include/fnum.h
 
 # status codes (fnum_status)
 OK = 0
 ERR_NO_DEVICE = 1
 ERR_INTERNAL = 21
 ERR_NOALLOC_TOO_LARGE = 24
+ERR_M_ELEMENTS = 25
 
 # window ids, normalisations, F-number kinds, flags (fnum.h)
 WINDOW_BOXCAR, WINDOW_HANN, WINDOW_TUKEY, WINDOW_TRIANGULAR = 0, 1, 2, 4
 NORM_OFF, NORM_ON, NORM_WINDOWED = 0, 1, 2
 F_DEFAULT, F_CONSTANT, F_ANGLE_LB, F_DISTANCE_CONSTANT, F_DISTANCE_NONE, F_DIRECTIVITY, F_SZABO = range(7)
 OBLIQUITY_RIGID, OBLIQUITY_SOFT = 0, 1
-FLAG_COMPOUND, FLAG_PLAIN_KERNEL, FLAG_SAFT_INTENDED = 0x1, 0x2, 0x4
+FLAG_COMPOUND, FLAG_PLAIN_KERNEL, FLAG_SAFT_INTENDED, FLAG_M_SEMANTICS = 0x1, 0x2, 0x4, 0x8
 
 _dp = C.POINTER(C.c_double)
 _fp = C.POINTER(C.c_float)
@@ -63,6 +65,7 @@ class PWDesc(C.Structure):
         ("f_number_values", _dp), ("n_f_number_values", C.c_int),
         ("normalization", C.c_int),
         ("device", C.c_int),
+        ("normalization_window", Window),
     ]
 
 
@@ -176,6 +179,8 @@ def lib():
     L.fnum_pw_plan_set_sound_speed.argtypes = [C.c_void_p, C.c_double]
     L.fnum_pw_sharpness_grad.restype = C.c_int
     L.fnum_pw_sharpness_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_int, _dp, _dp, C.c_void_p, C.c_void_p]
+    L.fnum_plan_m_signal.restype = C.c_int
+    L.fnum_plan_m_signal.argtypes = [C.c_void_p, _dp, _ip]
     L.fnum_bmode.restype = C.c_int
     L.fnum_bmode.argtypes = [C.c_void_p, C.c_longlong, C.c_int, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
     if L.fnum_abi_version() != ABI_VERSION:

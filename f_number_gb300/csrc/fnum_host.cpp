@@ -57,6 +57,7 @@ const StatusInfo kStatus[] = {
     {FNUM_ERR_RX_F_NUMBER, "InvalidRXFNumber", "Values of receive F-number must be nonnegative!"},
     {FNUM_ERR_NOALLOC_TOO_LARGE, "NoAllocScratchTooSmall",
      "Problem exceeds the 64 MiB static scratch of fnum_das_pw_noalloc!"},
+    {FNUM_ERR_M_ELEMENTS, "TooManyElements", "das_pw.m semantics support at most 256 array elements!"},
 };
 
 const StatusInfo* find_status(int s) {
@@ -300,6 +301,28 @@ int compute_band(const double* pz, int nz, int nt, int ne, double fs, double wid
   const int N_pad = (int)ceil((sqrt((double)ap2 + z1 * z1) - z1) * fs / c);
   const int N = nt + N_pad + 1 - ((nt + N_pad) % 2);
   const double f_lb = fb ? fb[0] : DBL_MIN, f_ub = fb ? fb[1] : fs / 2.0;
+  const int k_lb = (int)ceil(f_lb * N / fs);
+  const int k_ub = (int)floor(f_ub * N / fs);
+  if (!(k_lb > 0 && k_lb <= k_ub && k_ub < N / 2 + 1)) return FNUM_ERR_FREQUENCY_BOUNDS;
+  b->N = N;
+  b->k_lb = k_lb;
+  b->k_ub = k_ub;
+  b->K = k_ub - k_lb + 1;
+  b->coef = 2.0 * M_PI * fs / (N * c);
+  b->add = 2.0 * M_PI * t0 / N;
+  b->M = M;
+  return FNUM_OK;
+}
+
+// DFT order and band of das_pw.m (das_pw.m:340-362): padding from the first axial
+// position and the aperture in double; the same bin bounds
+int compute_band_m(const double* pz, int nt, int ne, double fs, double pitch, double c, const double* fb, double t0,
+                   Band* b) {
+  const double M = (ne - 1.0) / 2.0;
+  const double ap = pitch * ((ne - 1) - M) - pitch * (0 - M);
+  const int N_pad = (int)ceil((sqrt(ap * ap + pz[0] * pz[0]) - pz[0]) * fs / c);
+  const int N = nt + N_pad + 1 - ((nt + N_pad) % 2);
+  const double f_lb = fb ? fb[0] : DBL_EPSILON, f_ub = fb ? fb[1] : fs / 2.0;
   const int k_lb = (int)ceil(f_lb * N / fs);
   const int k_ub = (int)floor(f_ub * N / fs);
   if (!(k_lb > 0 && k_lb <= k_ub && k_ub < N / 2 + 1)) return FNUM_ERR_FREQUENCY_BOUNDS;
@@ -565,10 +588,17 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
   int s = check_pw(d, angles, na);
   if (s) return s;
   FNUM_CUDA(cudaSetDevice(d->device));
+  const bool msem = (flags & FNUM_FLAG_M_SEMANTICS) != 0;
+  if (msem && d->n_elements > fnum::M_MAXE) return FNUM_ERR_M_ELEMENTS;
   Band b;
-  if ((s = compute_band(d->positions_z, d->n_z, d->n_samples, d->n_elements, d->f_s, d->element_width,
-                        d->element_pitch, d->c_0, d->f_bounds, d->index_t0, &b)))
+  if (msem) {
+    if ((s = compute_band_m(d->positions_z, d->n_samples, d->n_elements, d->f_s, d->element_pitch, d->c_0,
+                            d->f_bounds, d->index_t0, &b)))
+      return s;
+  } else if ((s = compute_band(d->positions_z, d->n_z, d->n_samples, d->n_elements, d->f_s, d->element_width,
+                               d->element_pitch, d->c_0, d->f_bounds, d->index_t0, &b))) {
     return s;
+  }
   fnum_plan* P = new (std::nothrow) fnum_plan();
   if (!P) return FNUM_ERR_OUT_OF_MEMORY;
   P->kind = 0;
@@ -633,7 +663,40 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
     s = FNUM_ERR_CUDA;
     goto fail;
   }
-  {
+  if (msem) {
+    // das_pw.m semantics: double geometry and tables of pw_m_kernel (no segment scratch)
+    std::vector<double> mtx((size_t)3 * na), px(d->positions_x, d->positions_x + nx),
+        pz(d->positions_z, d->positions_z + nz);
+    for (int a = 0; a < na; ++a) {
+      const double ex = -sin(angles[a]), ez = cos(angles[a]);
+      const double c0 = d->element_pitch * (0 - b.M);
+      mtx[3 * a] = ex;
+      mtx[3 * a + 1] = ez;
+      mtx[3 * a + 2] = (ex > 0 ? 1.0 : (ex < 0 ? -1.0 : 0.0)) * c0;  // x_ref = sign(e_x) c_1 (das_pw.m:327)
+    }
+    double* dp;
+    if ((s = P->upload(&dp, px))) goto fail;
+    D.m_px = dp;
+    if ((s = P->upload(&dp, pz))) goto fail;
+    D.m_pz = dp;
+    if ((s = P->upload(&dp, mtx))) goto fail;
+    D.m_tx = dp;
+    if ((s = P->upload(&dp, P->F))) goto fail;
+    D.m_F0 = dp;
+    if ((s = P->alloc(&D.m_sig, (size_t)nz * b.K)) || (s = P->alloc(&D.m_sig_flag, (size_t)nz))) goto fail;
+    D.m_sem = 1;
+    D.m_norm = d->normalization == FNUM_NORMALIZATION_OFF ? 0 : (d->normalization == FNUM_NORMALIZATION_WINDOWED ? 2 : 1);
+    D.m_nwin_id = d->normalization_window.id;
+    D.m_nwin_par = (float)d->normalization_window.parameter;
+    D.m_c = d->c_0;
+    D.m_fs = d->f_s;
+    D.m_t0 = d->index_t0;
+    D.m_pitch = d->element_pitch;
+    D.m_width = d->element_width;
+    D.m_M = b.M;
+    P->grid = 0;
+    P->max_grid = 0;
+  } else {
     int bps = 0;
     P->grid = fnum::pw_fused_grid(D, &bps);
     // scratch for the largest grid of any kernel variant, so the autotuner may switch
@@ -804,6 +867,7 @@ int plan_beamform(fnum_plan* P, void* image, float* w, float* w2, cudaStream_t s
     return cuda_status(e);
   }
   const fnum::PWDev& D = P->pw;
+  if (D.m_sem) return cuda_status(fnum::launch_pw_m(D, P->n_out == 1, (float2*)image, w, st));
   if (P->n_out == 1) {
     cudaError_t e = plain ? fnum::launch_pw_plain(D, (float2*)image, w, st)
                           : fnum::launch_pw_fused(D, P->grid, (float2*)image, w, st);
@@ -1342,6 +1406,25 @@ int fnum_pw_sharpness_grad(fnum_plan* plan, const void* d_rf, int rf_is_double, 
   FNUM_CUDA(cudaStreamSynchronize(st));
   if (loss) *loss = -S[1] / (S[0] * S[0]);
   if (dloss_dc) *dloss_dc = g;
+  return FNUM_OK;
+}
+
+int fnum_plan_m_signal(const fnum_plan* plan, double* spectrum_re_im, int* has_signal) {
+  if (!plan || !spectrum_re_im || plan->kind != 0 || !plan->pw.m_sem) return FNUM_ERR_ARGUMENT;
+  FNUM_CUDA(cudaSetDevice(plan->device));
+  const fnum::PWDev& D = plan->pw;
+  std::vector<int> flag(D.nz);
+  FNUM_CUDA(cudaMemcpy(flag.data(), D.m_sig_flag, D.nz * sizeof(int), cudaMemcpyDeviceToHost));
+  int j = D.nz - 1;
+  while (j >= 0 && !flag[j]) --j;
+  if (has_signal) *has_signal = j >= 0;
+  std::vector<float2> sp(D.K, make_float2(0.0f, 0.0f));
+  if (j >= 0)
+    FNUM_CUDA(cudaMemcpy(sp.data(), D.m_sig + (size_t)j * D.K, D.K * sizeof(float2), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < D.K; ++k) {
+    spectrum_re_im[2 * k] = sp[k].x;
+    spectrum_re_im[2 * k + 1] = sp[k].y;
+  }
   return FNUM_OK;
 }
 

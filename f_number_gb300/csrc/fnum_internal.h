@@ -65,6 +65,16 @@ struct PWDev {
   const float* F_f;    // [K]
   const float4* tx_f;  // [na] {e_x, e_z, x_ref, 0}
   float M_f, pitch_f, coef_f, add_f;
+  // das_pw.m semantics (pw_m_kernel): double geometry, F before the depth cap
+  int m_sem;            // 1 = das_pw.m semantics
+  int m_norm;           // 0 off, 1 on, 2 windowed
+  int m_nwin_id; float m_nwin_par;   // window of the windowed normalisation
+  const double* m_px; const double* m_pz;
+  const double* m_tx;   // [na][3] e_x, e_z, x_ref
+  const double* m_F0;   // [K]
+  double m_c, m_fs, m_t0, m_pitch, m_width, m_M;
+  float2* m_sig;        // [nz][K] focused spectra of the last column (signal output)
+  int* m_sig_flag;      // [nz] 1 where the voxel has an active bin
 };
 
 struct SADev {
@@ -104,6 +114,8 @@ int pw_variant_of(const PWDev& d);
 int sa_fused_grid(const SADev& d, int* blocks_per_sm);
 cudaError_t launch_pw_fused(const PWDev& d, int grid, float2* image, float* weights, cudaStream_t s);
 cudaError_t launch_pw_plain(const PWDev& d, float2* image, float* weights, cudaStream_t s);
+constexpr int M_MAXE = 256;   // elements supported by the das_pw.m-semantics kernel
+cudaError_t launch_pw_m(const PWDev& d, int compound, float2* image, float* weights, cudaStream_t s);
 cudaError_t launch_sa_fused(const SADev& d, int grid, float2* image, float* wtx, float* wrx, cudaStream_t s);
 cudaError_t launch_sa_plain(const SADev& d, float2* image, float* wtx, float* wrx, cudaStream_t s);
 // sharpness-loss gradients of a compounded plane-wave plan (fnum_pw_sharpness_grad)

@@ -1575,3 +1575,163 @@ cudaError_t launch_pw_dldc(const PWDev& d, const float2* H, double coef, double*
 }
 
 }  // namespace fnum
+
+namespace fnum {
+
+// ---------------------------------------------------------------------------
+// das_pw.m semantics (the reference's CPU path, das_pw.m:310-481), per term:
+//   N_dft padded with the first axial position; F = min(F(p/lambda), sqrt(f z /
+//   (2.88 c))) per bin and depth (das_pw.m:371-377); 1-based aperture indices
+//   from z / (2F) in double; boxcar on the ideal half-width z / (2F), other
+//   windows on the element-edge half-widths over all elements without a cut-off
+//   (das_pw.m:436-452, windows' compute_samples_scalar); normalisation by the
+//   sum over elements, times the frequency window of normalizations.windowed
+//   (windowed.m:69-87); bins with an empty index range skipped (das_pw.m:403);
+//   spectra doubled (analytic signal) and no 2/N scaling (das_pw.m:384,467).
+// Phases are exact per term (cis_ku of the delay in cycles per bin, formed in
+// double).  One thread per voxel.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float win_m(int id, float par, float u) {
+  u = fabsf(u);
+  switch (id) {
+    case 0: return (u < 1.0f) ? 1.0f : 0.0f;
+    case 1: return 0.5f + 0.5f * cospif(u);
+    case 2: {
+      const float fr = 1.0f - par;
+      if (!(u < 1.0f)) return 0.0f;
+      return (u > fr) ? 0.5f * (1.0f + cospif((u - fr) / par)) : 1.0f;
+    }
+    case 4: return 1.0f - u;
+    default: return 0.0f;
+  }
+}
+
+struct MBin {
+  bool valid;
+  float inv_w;      // boxcar: 1 / (z / 2F)
+  float inv_l, inv_r;
+};
+
+__device__ __forceinline__ MBin m_bin(const PWDev& d, int kk, double x, double z) {
+  MBin b;
+  const int k = d.k_lb + kk;
+  const double f = d.m_fs * k / d.N_dft;
+  const double F = fmin(d.m_F0[kk], sqrt(f * z / (2.88 * d.m_c)));
+  const double w = z / (2.0 * F);
+  const double ilb = fmax(ceil(d.m_M + (x - w) / d.m_pitch) + 1.0, 1.0);
+  const double iub = fmin(floor(d.m_M + (x + w) / d.m_pitch) + 1.0, (double)d.ne);
+  b.valid = ilb <= iub;
+  b.inv_w = (float)(1.0 / w);
+  if (b.valid) {
+    const double lb = d.m_pitch * ((ilb - 1.0) - d.m_M) - d.m_width / 2.0;
+    const double ub = d.m_pitch * ((iub - 1.0) - d.m_M) + d.m_width / 2.0;
+    b.inv_l = (float)(1.0 / (x - lb));
+    b.inv_r = (float)(1.0 / (ub - x));
+  } else {
+    b.inv_l = b.inv_r = 0.0f;
+  }
+  return b;
+}
+
+// window sample of element e (dl = c_e - x) in bin b
+__device__ __forceinline__ float m_sample(const PWDev& d, const MBin& b, float dl) {
+  if (d.window_id == 0) return win_m(0, 0.0f, dl * b.inv_w);
+  return win_m(d.window_id, d.window_par, dl * ((dl < 0.0f) ? b.inv_l : b.inv_r));
+}
+
+__global__ void __launch_bounds__(NTHREADS) pw_m_kernel(const PWDev d, int compound, float2* __restrict__ image,
+                                                        float* __restrict__ weights) {
+  const int i = blockIdx.x * TILE_X + (threadIdx.x >> 5);
+  const int j = blockIdx.y * TILE_Z + (threadIdx.x & 31);
+  if (i >= d.nx || j >= d.nz) return;
+  const double x = d.m_px[i], z = d.m_pz[j];
+  dfl ue[M_MAXE];
+  float dlf[M_MAXE];
+  int cnt[M_MAXE];
+  const bool last_col = (i == d.nx - 1) && d.m_sig;
+  bool any_valid = false;
+  float2 tot = make_float2(0.0f, 0.0f), tcomp = make_float2(0.0f, 0.0f);
+  for (int e = 0; e < d.ne; ++e) dlf[e] = (float)(d.m_pitch * (e - d.m_M) - x);
+  for (int a = 0; a < d.na; ++a) {
+    const double ex = d.m_tx[3 * a], ez = d.m_tx[3 * a + 1], xref = d.m_tx[3 * a + 2];
+    const double dtx = ex * (x - xref) + ez * z;
+    for (int e = 0; e < d.ne; ++e) {
+      const double dl = d.m_pitch * (e - d.m_M) - x;
+      const double tof = dtx / d.m_c + d.m_t0 / d.m_fs + sqrt(dl * dl + z * z) / d.m_c;
+      const double u = tof * d.m_fs / d.N_dft;  // cycles per bin
+      const float hi = (float)u;
+      ue[e] = make_float2(hi, (float)(u - (double)hi));
+    }
+    if (d.m_norm == 2) {  // windowed: bins at which each element's normalised sample is positive
+      for (int e = 0; e < d.ne; ++e) cnt[e] = 0;
+      for (int kk = 0; kk < d.K; ++kk) {
+        const MBin b = m_bin(d, kk, x, z);
+        if (!b.valid) continue;
+        float W = 0.0f;
+        for (int e = 0; e < d.ne; ++e) W += m_sample(d, b, dlf[e]);
+        for (int e = 0; e < d.ne; ++e) cnt[e] += (m_sample(d, b, dlf[e]) / W > 0.0f) ? 1 : 0;
+      }
+    }
+    float2 acc = make_float2(0.0f, 0.0f), comp = make_float2(0.0f, 0.0f);
+    int idx = 0;
+    for (int kk = 0; kk < d.K; ++kk) {
+      const MBin b = m_bin(d, kk, x, z);
+      if (!b.valid) {
+        if (last_col) d.m_sig[(size_t)j * d.K + kk] = make_float2(0.0f, 0.0f);
+        continue;
+      }
+      any_valid = true;
+      const int k = d.k_lb + kk;
+      float invW = 1.0f;
+      if (d.m_norm != 0) {
+        float W = 0.0f;
+        for (int e = 0; e < d.ne; ++e) W += m_sample(d, b, dlf[e]);
+        invW = 1.0f / W;
+      }
+      float2 S = make_float2(0.0f, 0.0f);
+      for (int e = 0; e < d.ne; ++e) {
+        float ws = m_sample(d, b, dlf[e]) * invW;
+        if (d.m_norm == 2) {
+          const float h = 0.5f * (float)cnt[e];
+          ws *= win_m(d.m_nwin_id, d.m_nwin_par, ((float)idx - h) / h);
+        }
+        const float2 X = d.X[((size_t)e * d.K + kk) * d.x_na + d.x_a0 + a];
+        const float2 ph = cis_ku(k, ue[e]);
+        const float2 t = cmul(ph, X);
+        S.x = fmaf(2.0f * ws, t.x, S.x);
+        S.y = fmaf(2.0f * ws, t.y, S.y);
+      }
+      if (last_col) d.m_sig[(size_t)j * d.K + kk] = S;
+      float y = S.x - comp.x, tt = acc.x + y;
+      comp.x = (tt - acc.x) - y;
+      acc.x = tt;
+      y = S.y - comp.y;
+      tt = acc.y + y;
+      comp.y = (tt - acc.y) - y;
+      acc.y = tt;
+      ++idx;
+    }
+    if (compound) {
+      float y = acc.x - tcomp.x, tt = tot.x + y;
+      tcomp.x = (tt - tot.x) - y;
+      tot.x = tt;
+      y = acc.y - tcomp.y;
+      tt = tot.y + y;
+      tcomp.y = (tt - tot.y) - y;
+      tot.y = tt;
+    } else {
+      image[((size_t)a * d.nx + i) * d.nz + j] = acc;
+    }
+  }
+  if (compound) image[(size_t)i * d.nz + j] = tot;
+  if (weights) weights[(size_t)i * d.nz + j] = 0.0f;
+  if (last_col) d.m_sig_flag[j] = any_valid ? 1 : 0;
+}
+
+cudaError_t launch_pw_m(const PWDev& d, int compound, float2* image, float* weights, cudaStream_t s) {
+  dim3 grid((d.nx + TILE_X - 1) / TILE_X, (d.nz + TILE_Z - 1) / TILE_Z);
+  pw_m_kernel<<<grid, NTHREADS, 0, s>>>(d, compound, image, weights);
+  return cudaGetLastError();
+}
+
+}  // namespace fnum

@@ -98,6 +98,18 @@ def _band_pl(pz, nt, ne, f_s, width, pitch, c_0, fb, t0):
     return pitch * np.arange(k_lb, k_ub + 1) * f_s / (N * c_0)
 
 
+def _band_m(pz, nt, ne, f_s, pitch, c_0, fb):
+    """DFT order and band bins of das_pw.m (das_pw.m:340-362): padding from the first
+    axial position, aperture in double."""
+    M = (ne - 1) / 2.0
+    ap = pitch * ((ne - 1) - M) - pitch * (0 - M)
+    z0 = float(np.asarray(pz, dtype=np.float64).ravel()[0])
+    n_pad = int(math.ceil((math.sqrt(ap * ap + z0 * z0) - z0) * f_s / c_0))
+    N = nt + n_pad + 1 - ((nt + n_pad) % 2)
+    f_lb, f_ub = (np.finfo(np.float64).eps, f_s / 2.0) if fb is None else (float(fb[0]), float(fb[1]))
+    return N, int(math.ceil(f_lb * N / f_s)), int(math.floor(f_ub * N / f_s))
+
+
 # ---------------------------------------------------------------------------
 # MEX gateways
 # ---------------------------------------------------------------------------
@@ -289,11 +301,12 @@ def das_pw(positions_x, positions_z, data_RF, f_s, steering_angle, element_width
            f_bounds=None, index_t0=None, window=None, F_number=None, normalization=None, platform=None):
     """Fourier-domain DAS for one steered plane wave (``das_pw.m``).
 
-    Returns the complex image [N_z, N_x] of the ``platforms.gpu`` path (the
-    MEX output: single precision, scaled by 2/N_dft).  Defaults follow
-    ``das_pw.m:207-283`` except ``platform``, which defaults to ``gpu(0)``:
-    this package implements the GPU path, and ``platforms.cpu`` (the
-    reference's MATLAB loop) raises ``das_pw:CPUPathNotProvided``."""
+    ``platforms.gpu`` (the default here, ``gpu(0)``) returns the complex image
+    [N_z, N_x] of the MEX path (single precision, scaled by 2/N_dft), as
+    das_pw.m does.  ``platforms.cpu`` returns what das_pw.m's own loop returns --
+    (image, F_number_values, signal) with its semantics (das_pw.m:310-481) --
+    computed on GPU 0 by the das_pw.m-semantics kernel: there is no CPU compute
+    path.  Defaults follow ``das_pw.m:207-283``."""
     fn = "das_pw"
     _check_common_m(fn, positions_x, positions_z, f_s)
     rf = np.asarray(data_RF)
@@ -329,11 +342,35 @@ def das_pw(positions_x, positions_z, data_RF, f_s, steering_angle, element_width
     if not isinstance(platform, _plat.platform):
         _err(fn + ":NoPlatform", "platform must be scalar platforms.platform!")
     if not isinstance(platform, _plat.gpu):
-        _err(fn + ":CPUPathNotProvided",
-             "platforms.cpu is the reference's MATLAB implementation; this package provides platforms.gpu")
+        return _das_pw_m(positions_x, positions_z, rf, f_s_v, th, w, p, c, fb, t0, window, F_number, normalization)
     image, _ = gpu_bf_das_pw_rf(positions_x, positions_z, rf, f_s_v, th, w, p, c, fb, t0, window, F_number,
                                 normalization, platform.index)
     return image
+
+
+def _das_pw_m(positions_x, positions_z, rf, f_s, th, width, pitch, c_0, fb, t0, window, F_number, normalization):
+    """platforms.cpu of das_pw: the semantics of das_pw.m's own loop (das_pw.m:310-481),
+    computed on GPU 0 by the das_pw.m-semantics kernel.  Returns (image [N_z, N_x]
+    complex128 as das_pw.m, F_number_values [n_bins, N_z] (capped per depth,
+    das_pw.m:371-377), signal (das_pw.m:477-481))."""
+    import torch
+    px = np.asarray(positions_x, dtype=np.float64).ravel()
+    pz = np.asarray(positions_z, dtype=np.float64).ravel()
+    nt, ne = rf.shape
+    plan = PWPlan(px, pz, nt, ne, f_s, [th], width, pitch, c_0, fb, t0, window, F_number, normalization, device=0,
+                  compound=True, semantics="m")
+    try:
+        rf_d = torch.tensor(np.ascontiguousarray(rf.T), dtype=torch.float64, device="cuda:0")
+        img = plan.execute(rf_d)
+        torch.cuda.synchronize()
+        image = img[0].cpu().numpy().T.astype(np.complex128)
+        inf = plan.info()
+        f = f_s * np.arange(inf["k_lb"], inf["k_ub"] + 1) / inf["N_dft"]
+        F0 = plan.f_numbers()
+        F = np.minimum(F0[:, None], np.sqrt(f[:, None] * pz[None, :] / (2.88 * c_0)))
+        return image, F, plan.m_signal()
+    finally:
+        plan.close()
 
 
 def das_sa(positions_x, positions_z, data_RF, f_s, element_width, element_pitch, c_0, f_bounds=None, index_t0=None,
@@ -457,7 +494,12 @@ class PWPlan(_Plan):
 
     def __init__(self, positions_x, positions_z, n_samples, n_elements, f_s, steering_angles, element_width,
                  element_pitch, c_0, f_bounds=None, index_t0=0.0, window=None, F_number=None, normalization=None,
-                 device=0, compound=True, kernel="fused"):
+                 device=0, compound=True, kernel="fused", semantics="mex"):
+        """semantics: "mex" (the reference's GPU gateway, the default) or "m" (its CPU
+        path das_pw.m: see FNUM_FLAG_M_SEMANTICS; images are not scaled by 2/N_dft)."""
+        if semantics not in ("mex", "m"):
+            raise ValueError("semantics must be 'mex' or 'm'")
+        self.semantics = semantics
         self._px = np.ascontiguousarray(np.asarray(positions_x, dtype=np.float64).ravel())
         self._pz = np.ascontiguousarray(np.asarray(positions_z, dtype=np.float64).ravel())
         self._angles = np.ascontiguousarray(np.atleast_1d(np.asarray(steering_angles, dtype=np.float64)).ravel())
@@ -471,14 +513,21 @@ class PWPlan(_Plan):
         d.f_bounds = _lib.dptr(self._fb)
         d.index_t0 = float(index_t0)
         d.window = _window_struct(window, "gpu_bf_das_pw_rf:InvalidWindow")
-        pl = _band_pl(self._pz, n_samples, n_elements, f_s, element_width, element_pitch, c_0, self._fb,
-                      index_t0) if F_number is not None else None
+        if semantics == "m":
+            Nm, klm, kum = _band_m(self._pz, int(n_samples), int(n_elements), f_s, element_pitch, c_0, self._fb)
+            pl = element_pitch * np.arange(klm, kum + 1) * f_s / (Nm * c_0) if F_number is not None else None
+        else:
+            pl = _band_pl(self._pz, n_samples, n_elements, f_s, element_width, element_pitch, c_0, self._fb,
+                          index_t0) if F_number is not None else None
         d.f_number, self._fvals = _f_number_args(F_number, pl)
         if self._fvals is not None:
             d.f_number_values, d.n_f_number_values = _lib.dptr(self._fvals), self._fvals.size
         d.normalization = _norm_code(normalization, "gpu_bf_das_pw_rf:InvalidNormalization")
+        if isinstance(normalization, _norm.windowed):
+            d.normalization_window = normalization.window.c_struct()
         d.device = int(device)
-        flags = (_lib.FLAG_COMPOUND if compound else 0) | (_lib.FLAG_PLAIN_KERNEL if kernel == "plain" else 0)
+        flags = (_lib.FLAG_COMPOUND if compound else 0) | (_lib.FLAG_PLAIN_KERNEL if kernel == "plain" else 0) | (
+            _lib.FLAG_M_SEMANTICS if semantics == "m" else 0)
         ptr = _lib.C.c_void_p()
         _lib.check(_lib.lib().fnum_pw_plan_create(_lib.C.byref(d), _lib.dptr(self._angles), self._angles.size, flags,
                                                   _lib.C.byref(ptr)))
@@ -487,6 +536,24 @@ class PWPlan(_Plan):
         self.n_x, self.n_z, self.n_bins = inf["n_x"], inf["n_z"], inf["n_bins"]
         self.n_elements, self.n_angles = inf["n_elements"], inf["n_angles"]
         self.n_out = 1 if compound else self._angles.size
+
+
+def _pw_m_signal(self):
+    """das_pw.m's `signal` output after an execute of a plan with semantics="m": the
+    inverse DFT (length N_dft) of the focused spectrum of the last voxel processed
+    (das_pw.m:477-481), or None when that column has no active bin."""
+    inf = self.info()
+    spec = np.zeros(2 * self.n_bins, dtype=np.float64)
+    has = _lib.C.c_int(0)
+    _lib.check(_lib.lib().fnum_plan_m_signal(self._ptr, _lib.dptr(spec), _lib.C.byref(has)))
+    if not has.value:
+        return None
+    full = np.zeros(inf["N_dft"], dtype=np.complex128)
+    full[inf["k_lb"]:inf["k_ub"] + 1] = spec[0::2] + 1j * spec[1::2]
+    return np.fft.ifft(full, inf["N_dft"])
+
+
+PWPlan.m_signal = _pw_m_signal
 
 
 def _pw_set_sound_speed(self, c_0):

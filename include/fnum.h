@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define FNUM_ABI_VERSION 2
+#define FNUM_ABI_VERSION 3
 
 typedef enum fnum_status {
   FNUM_OK = 0,
@@ -59,7 +59,8 @@ typedef enum fnum_status {
   FNUM_ERR_INTERNAL = 21,          /* device-side consistency check failed */
   FNUM_ERR_TX_F_NUMBER = 22,       /* gpu_bf_saft_rf:InvalidTXFNumber */
   FNUM_ERR_RX_F_NUMBER = 23,       /* gpu_bf_saft_rf:InvalidRXFNumber */
-  FNUM_ERR_NOALLOC_TOO_LARGE = 24  /* fnum_das_pw_noalloc: problem exceeds FNUM_NOALLOC_SCRATCH_BYTES */
+  FNUM_ERR_NOALLOC_TOO_LARGE = 24, /* fnum_das_pw_noalloc: problem exceeds FNUM_NOALLOC_SCRATCH_BYTES */
+  FNUM_ERR_M_ELEMENTS = 25         /* FNUM_FLAG_M_SEMANTICS: more than 256 elements */
 } fnum_status;
 
 /* window ids follow the MEX mapping (+cuda/gpu_bf_helper_functions.cu:56-97) */
@@ -105,6 +106,13 @@ typedef struct fnum_f_number {
 #define FNUM_FLAG_COMPOUND        0x1  /* PW: sum the images of all angles into one image */
 #define FNUM_FLAG_PLAIN_KERNEL    0x2  /* use the per-voxel FP32 kernel (reference arithmetic) */
 #define FNUM_FLAG_SAFT_INTENDED   0x4  /* SA: divide by whichever sums are on, always accumulate */
+/* PW: the semantics of the reference's CPU path (das_pw.m:310-481) instead of
+   the MEX's: N_dft padded with positions_z[0]; F capped at sqrt(f z / (2.88 c))
+   per bin and depth; boxcar on the ideal half-width; other windows over all
+   elements without a cut-off; normalizations.windowed applied with
+   normalization_window; image not scaled by 2/N_dft (spectra doubled).  Up to
+   256 elements.  Weights outputs are written as 0. */
+#define FNUM_FLAG_M_SEMANTICS     0x8
 
 /* --- information ------------------------------------------------------ */
 int fnum_abi_version(void);
@@ -144,6 +152,7 @@ typedef struct fnum_pw_desc {
   int n_f_number_values;
   int normalization;               /* fnum_normalization */
   int device;
+  fnum_window normalization_window; /* frequency window of normalizations.windowed (FNUM_FLAG_M_SEMANTICS) */
 } fnum_pw_desc;
 
 /* One call = the reference's gpu_bf_das_pw_rf for each steering angle
@@ -257,6 +266,13 @@ int fnum_batch_create(fnum_plan* const* plans, int n, const void* const* d_rf, c
 int fnum_batch_execute(fnum_batch* batch, void* stream);
 int fnum_batch_frame_times(const fnum_batch* batch, float* ms);
 int fnum_batch_destroy(fnum_batch* batch);
+
+/* After an execute of a plan with FNUM_FLAG_M_SEMANTICS: the focused spectrum of
+   the last voxel das_pw.m processes (last column, deepest voxel with an active
+   bin), complex interleaved per band bin (0 at bins without an active aperture);
+   das_pw.m returns its inverse DFT as `signal` (das_pw.m:477-481).  *has_signal
+   is 0 when no voxel of the last column has an active bin. */
+int fnum_plan_m_signal(const fnum_plan* plan, double* spectrum_re_im, int* has_signal);
 
 /* --- image-sharpness gradients (no counterpart in the reference) --------- */
 /* Re-times a plane-wave plan's phase tables at sound speed c_0.  The DFT

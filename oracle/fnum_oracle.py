@@ -510,7 +510,10 @@ def das_pw_m(positions_x, positions_z, data_rf, f_s, steering_angle, element_wid
     other windows on the element-edge widths without a cut-off
     (``das_pw.m:449-452``), ``normalizations.windowed`` applied
     (``+normalizations/windowed.m:69-87``), frequencies with an empty index
-    range skipped (``das_pw.m:403``), no 2/N scaling (``das_pw.m:384,467``)."""
+    range skipped (``das_pw.m:403``), no 2/N scaling (``das_pw.m:384,467``).
+    info["F_capped"] is the [K, Z] F-number table actually used
+    (``das_pw.m:371-377``); info["signal"] the inverse DFT of the last processed
+    voxel's focused spectrum (``das_pw.m:477-481``)."""
     px = np.asarray(positions_x, dtype=np.float64).ravel()
     pz = np.asarray(positions_z, dtype=np.float64).ravel()
     rf = np.asarray(data_rf, dtype=np.float64)
@@ -579,8 +582,18 @@ def das_pw_m(positions_x, positions_z, data_rf, f_s, steering_angle, element_wid
                     n_over_two = (ws > 0).sum(axis=0) / 2.0
                     idx = np.arange(ws.shape[0])[:, None]
                     ws = ws * window_m(fwin, (idx - n_over_two[None, :]) / n_over_two[None, :])
-            image[iz, ix] = np.sum(ws * wts * Xa[v, :])
-    return image, {"N_dft": N, "k_lb": int(ks[0]), "k_ub": int(ks[-1]), "F": F0}
+            focused = np.sum(ws * wts * Xa[v, :], axis=1)               # [Kv]
+            image[iz, ix] = np.sum(focused)
+            last = (ks[v], focused)
+    # signal of the last voxel processed (das_pw.m:477-481): its focused spectrum at the
+    # active bins of a length-N spectrum, inverse DFT
+    signal = None
+    if want is None and px.size and 'last' in locals():
+        spec = np.zeros(N, dtype=np.complex128)
+        spec[last[0]] = last[1]
+        signal = np.fft.ifft(spec, N)
+    return image, {"N_dft": N, "k_lb": int(ks[0]), "k_ub": int(ks[-1]), "F": F0, "F_capped": Fv,
+                   "signal": signal}
 
 
 # ---------------------------------------------------------------------------
