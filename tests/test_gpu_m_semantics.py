@@ -44,10 +44,20 @@ def test_m_semantics_matches_oracle(gpu, win, norm):
                                  norm, platforms.cpu())
         ref, info = O.das_pw_m(px, pz, rf, 20e6, angle, arr.width, arr.pitch, 1540.0, (2e6, 7e6), 0.0, win.spec(),
                                fn.spec(), _norm_spec(norm))
-        assert np.linalg.norm(img - ref) / np.linalg.norm(ref) < TOL_L2, (fn.string(),)
+        # normalizations.windowed divides by each element's half-count of bins with a
+        # positive weight; where an element has none, MATLAB (and the oracle) give
+        # 0 * NaN = NaN.  The GPU must give NaN at the same voxels.
+        bad = ~np.isfinite(ref)
+        assert np.array_equal(~np.isfinite(img), bad), (fn.string(),)
+        if (~bad).any():
+            assert np.linalg.norm(img[~bad] - ref[~bad]) / np.linalg.norm(ref[~bad]) < TOL_L2, (fn.string(),)
         np.testing.assert_allclose(F, info["F_capped"], rtol=1e-12)
         assert sig is not None and info["signal"] is not None
-        assert np.linalg.norm(sig - info["signal"]) / np.linalg.norm(info["signal"]) < TOL_L2
+        sbad = ~np.isfinite(info["signal"])
+        assert np.array_equal(~np.isfinite(sig), sbad)
+        if (~sbad).any():
+            s_ok, r_ok = sig[~sbad], info["signal"][~sbad]
+            assert np.linalg.norm(s_ok - r_ok) / np.linalg.norm(r_ok) < TOL_L2
 
 
 def test_m_semantics_band_and_scaling(gpu):
