@@ -1218,13 +1218,245 @@ sa_fused_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
   }
 }
 
+// Synthetic-aperture recurrence for a boxcar receive window.  A receive
+// element is then either out of the aperture or in it with the weight
+// f = a_tx(t) / (W_tx W_rx) shared by the whole pass, so a segment boundary
+// reduces to the new f and the mask of the pass's receive elements that are
+// in.  Ahead of the recurrence each lane resolves its own boundaries of the
+// next SA_EV_BINS bins into a table {f, mask} in shared memory (a column per
+// lane) and a bit mask of the bins that carry one; the bin loop only applies
+// them: one common rescale ratio for the elements that stay in, zero for the
+// ones that enter, a flush for the ones that leave.  The boundary work is done
+// per lane instead of per bin of the warp, and the arithmetic is that of
+// sa_fused_kernel with a boxcar receive window.
+constexpr int SA_EV_BINS = 32;
+
+template <int EPT, int WT>
+__global__ void __launch_bounds__(NTHREADS, 4)
+sa_event_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ wtx_out, float* __restrict__ wrx_out,
+                int n_tiles_x, int n_tiles_z, int weights_only) {
+  static_assert(EPT <= 31, "receive mask");
+  constexpr int ROW = (EPT + 1) & ~1;
+  __shared__ __align__(16) float2 xs[2][KCHUNK * ROW];
+  __shared__ float2 ev[SA_EV_BINS][NTHREADS];        // {f from the bin on, receive mask}
+  __shared__ int ranges[4];
+  __shared__ int s_tile;
+  __shared__ unsigned long long s_count[2];          // active terms, zero-weight bins
+  extern __shared__ __align__(16) unsigned char dyn[];  // lb[ne], ub[ne] (dfl), ktop_tx[ne], ktop_rx[ne]
+  dfl* lb_s = (dfl*)dyn;
+  dfl* ub_s = lb_s + d.ne;
+  int* ktop_tx = (int*)(ub_s + d.ne);
+  int* ktop_rx = ktop_tx + d.ne;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int n_tiles = n_tiles_x * n_tiles_z;
+  int4* seg = d.seg + ((size_t)blockIdx.x * NTHREADS + tid) * (size_t)d.seg_cap * SA_SEG_INT4;
+  const float ipt = (d.wtx_par > 0.0f) ? 1.0f / d.wtx_par : 0.0f;
+  unsigned long long n_exec = 0;
+  if (tid == 0) s_count[0] = s_count[1] = 0ull;
+  for (int e = tid; e < d.ne; e += NTHREADS) {
+    lb_s[e] = d.el_lb[e];
+    ub_s[e] = d.el_ub[e];
+  }
+
+  for (;;) {
+    if (tid == 0) s_tile = (int)atomicAdd(&d.counters[3], 1ull);
+    for (int e = tid; e < 2 * d.ne; e += NTHREADS) ktop_tx[e] = -1;
+    if (tid == 0) {
+      ranges[0] = ranges[2] = d.ne;
+      ranges[1] = ranges[3] = -1;
+    }
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= n_tiles) break;
+    int tx_, tz_;
+    tile_coords(tile, n_tiles_x, n_tiles_z, tx_, tz_);
+    const int i = tx_ * TILE_X + warp;
+    const int j = tz_ * TILE_Z + lane;
+    const bool valid = (i < d.nx) && (j < d.nz);
+    const int ic = min(i, d.nx - 1), jc = min(j, d.nz - 1);
+    int nseg;
+    {
+      float Wtx_top, Wrx_top;
+      unsigned long long n_active = 0, n_empty = 0;
+      nseg = sa_build_segments(d, ic, jc, valid, seg, ktop_tx, ktop_rx, ranges, Wtx_top, Wrx_top, n_active, n_empty);
+      atomicAdd(&s_count[0], n_active);
+      atomicAdd(&s_count[1], n_empty);
+      if (valid) {
+        if (wtx_out) wtx_out[(size_t)ic * d.nz + jc] = Wtx_top;
+        if (wrx_out) wrx_out[(size_t)ic * d.nz + jc] = Wrx_top;
+      }
+    }
+    __syncthreads();
+    const int T_lo = ranges[0], T_hi = weights_only ? -1 : ranges[1], R_lo = ranges[2], R_hi = ranges[3];
+
+    const dfl xm = d.col_m[ic], xu = d.col_u[ic], zu2 = d.row_u2[jc];
+    const int emid = d.col_emid[ic];
+    float2 acc = make_float2(0.0f, 0.0f), comp = make_float2(0.0f, 0.0f);
+
+    for (int t = T_lo; t <= T_hi; ++t) {
+      const int kt_t = ktop_tx[t];
+      if (kt_t < d.k_lb) continue;
+      const dfl ctm = d.el_m[t];
+      const float dxt = fabsf((ctm.x - xm.x) + (ctm.y - xm.y));
+      const dfl utx = df_sqrt(df_add(df_sqr(df_sub(d.el_u[t], xu)), zu2));
+      for (int r0 = R_lo; r0 <= R_hi; r0 += EPT) {
+        int kt = -1;
+#pragma unroll
+        for (int q = 0; q < EPT; ++q)
+          if (r0 + q <= R_hi) kt = max(kt, ktop_rx[r0 + q]);
+        kt = min(kt, kt_t);
+        if (kt < d.k_lb) continue;
+        if (tid == 0) n_exec += (unsigned long long)(kt - d.k_lb + 1) * EPT * NTHREADS;
+        // receive elements r0 + q in [m_lo, m_hi] form the mask of an aperture
+        const int m_hi_cap = min(R_hi, r0 + EPT - 1);
+        auto rx_mask = [&](int rcode) -> unsigned {
+          const int lo = max(min(code_ilb(rcode), emid), r0);
+          const int hi = min(max(code_iub(rcode), emid - 1), m_hi_cap);
+          return (lo <= hi) ? ((2u << (hi - r0)) - (1u << (lo - r0))) : 0u;
+        };
+        float2 z[EPT], A[EPT];
+#pragma unroll
+        for (int q = 0; q < EPT; ++q) {
+          const int e = min(r0 + q, d.ne - 1);
+          z[q] = cis_ku(1, df_add(df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2)), utx));
+          A[q] = make_float2(0.0f, 0.0f);
+        }
+        // segment in effect at kt, and the state of the boundary pre-pass:
+        // tx code and tx window value of the last resolved entry
+        int s = 0;
+        int4 cur = make_int4(-1, seg_code(d.ne, -1), seg_code(d.ne, -1), 0);
+        if (nseg > 0) {
+          s = sa_seg_find(seg, nseg, kt);
+          cur = seg[s];
+        }
+        int4 ring[SEG_RING];
+#pragma unroll
+        for (int r = 0; r < SEG_RING; ++r) ring[r] = seg[min(s + 1 + r, nseg)];
+        int p_ct = cur.y;
+        float p_at = sa_apod<WT>(lb_s, ub_s, xm, t, emid, code_ilb(cur.y), code_iub(cur.y), dxt, d.wtx_par, ipt);
+        float f = p_at * __int_as_float(cur.w);
+        unsigned m = (f != 0.0f) ? rx_mask(cur.z) : 0u;
+
+        float2 part = make_float2(0.0f, 0.0f);
+        const int c_top = (kt - d.k_lb) / KCHUNK;
+        __syncthreads();  // every thread is done with both buffers of the previous pass
+        sa_stage_chunk<EPT>(xs[0], d, t, r0, d.k_lb + c_top * KCHUNK, kt - (d.k_lb + c_top * KCHUNK) + 1, tid);
+        int buf = 0;
+        for (int chunk = c_top; chunk >= 0; --chunk) {
+          const int kc_lo = d.k_lb + chunk * KCHUNK;
+          const int kc_hi = (chunk == c_top) ? kt : kc_lo + KCHUNK - 1;
+          cp_async_wait_all();
+          __syncthreads();
+          if (chunk > 0) sa_stage_chunk<EPT>(xs[buf ^ 1], d, t, r0, kc_lo - KCHUNK, KCHUNK, tid);
+          const float2* xb = xs[buf];
+          buf ^= 1;
+          for (int ks_hi = kc_hi; ks_hi >= kc_lo; ks_hi -= SA_EV_BINS) {
+            const int ks_lo = max(kc_lo, ks_hi - (SA_EV_BINS - 1));
+            // this lane's boundaries in bins ks_lo .. ks_hi (entries sorted by
+            // k_start, descending; the sentinel's bin -1 ends the walk)
+            unsigned emask = 0u;
+            while (ring[0].x >= ks_lo) {
+              const int4 c = ring[0];
+#pragma unroll
+              for (int r = 0; r + 1 < SEG_RING; ++r) ring[r] = ring[r + 1];
+              ++s;
+              ring[SEG_RING - 1] = seg[min(s + SEG_RING, nseg)];
+              if (c.y != p_ct || p_at == 0.0f)
+                p_at = sa_apod<WT>(lb_s, ub_s, xm, t, emid, code_ilb(c.y), code_iub(c.y), dxt, d.wtx_par, ipt);
+              p_ct = c.y;
+              const float fn = p_at * __int_as_float(c.w);
+              const unsigned mn = (fn != 0.0f) ? rx_mask(c.z) : 0u;
+              ev[c.x - ks_lo][tid] = make_float2(fn, __uint_as_float(mn));
+              emask |= 1u << (c.x - ks_lo);
+            }
+            int nev = emask ? ks_lo + 31 - __clz(emask) : -1;
+            for (int k = ks_hi; k >= ks_lo; --k) {
+              if (k == nev) {
+                const float2 en = ev[k - ks_lo][tid];
+                const float fn = en.x;
+                const unsigned mn = __float_as_uint(en.y);
+                const unsigned leave = m & ~mn, stay = m & mn;
+                if (leave) {  // receive elements that leave the aperture below k+1: flush at k+1
+#pragma unroll
+                  for (int q = 0; q < EPT; ++q) {
+                    if ((leave >> q) & 1u) {
+                      const dfl u = df_add(df_sqrt(df_add(df_sqr(df_sub(d.el_u[r0 + q], xu)), zu2)), utx);
+                      const float2 tt = cmul(cis_ku(k + 1, u), A[q]);
+                      part.x = fmaf(f, tt.x, part.x);
+                      part.y = fmaf(f, tt.y, part.y);
+                    }
+                  }
+                }
+                const float r = stay ? __fdividef(f, fn) : 0.0f;
+                if (stay == m && mn == m) {
+#pragma unroll
+                  for (int q = 0; q < EPT; ++q) {
+                    A[q].x *= r;
+                    A[q].y *= r;
+                  }
+                } else {
+#pragma unroll
+                  for (int q = 0; q < EPT; ++q) {
+                    const bool st = (stay >> q) & 1u;
+                    A[q].x = st ? A[q].x * r : 0.0f;
+                    A[q].y = st ? A[q].y * r : 0.0f;
+                  }
+                }
+                f = fn;
+                m = mn;
+                emask &= ~(1u << (k - ks_lo));
+                nev = emask ? ks_lo + 31 - __clz(emask) : -1;
+              }
+              const float2* xr = &xb[(k - kc_lo) * ROW];
+#pragma unroll
+              for (int q = 0; q < EPT; ++q) {
+                const float2 x = xr[q];
+                const float2 Aq = A[q], zq = z[q];
+                A[q].x = fmaf(Aq.x, zq.x, fmaf(-Aq.y, zq.y, x.x));
+                A[q].y = fmaf(Aq.x, zq.y, fmaf(Aq.y, zq.x, x.y));
+              }
+            }
+          }
+          if (chunk % d.flush_chunks == 0) {
+#pragma unroll
+            for (int q = 0; q < EPT; ++q) {
+              if ((m >> q) & 1u) {
+                const dfl u = df_add(df_sqrt(df_add(df_sqr(df_sub(d.el_u[r0 + q], xu)), zu2)), utx);
+                const float2 tt = cmul(cis_ku(kc_lo, u), A[q]);
+                part.x = fmaf(f, tt.x, part.x);
+                part.y = fmaf(f, tt.y, part.y);
+              }
+              A[q] = make_float2(0.0f, 0.0f);
+            }
+          }
+        }
+        float y = part.x - comp.x, tt = acc.x + y;
+        comp.x = (tt - acc.x) - y;
+        acc.x = tt;
+        y = part.y - comp.y;
+        tt = acc.y + y;
+        comp.y = (tt - acc.y) - y;
+        acc.y = tt;
+      }
+    }
+    if (valid) image[(size_t)ic * d.nz + jc] = make_float2(acc.x * d.scale, acc.y * d.scale);
+    __syncthreads();
+  }
+  if (tid == 0) {
+    atomicAdd(&d.counters[0], s_count[0]);
+    atomicAdd(&d.counters[1], s_count[1]);
+    atomicAdd(&d.counters[4], n_exec);
+  }
+}
+
 constexpr int SA_EPT = 8;
 typedef void (*sa_kernel_t)(const SADev, float2*, float*, float*, int, int, int);
 
 template <int WT>
 static sa_kernel_t sa_pick_rx(int wr) {
   switch (wr) {
-    case 0: return sa_fused_kernel<SA_EPT, WT, 0>;
+    case 0: return sa_event_kernel<SA_EPT, WT>;   // boxcar receive window
     case 1: return sa_fused_kernel<SA_EPT, WT, 1>;
     case 2: return sa_fused_kernel<SA_EPT, WT, 2>;
     default: return sa_fused_kernel<SA_EPT, WT, 4>;
