@@ -18,7 +18,7 @@ EXPORTS = (
     "fnum_plan_info_get", "fnum_plan_f_numbers", "fnum_plan_destroy", "fnum_diag_fp32_peak",
     "fnum_das_pw_noalloc", "fnum_bmode", "fnum_plan_autotune", "fnum_batch_create", "fnum_batch_execute",
     "fnum_batch_frame_times", "fnum_batch_destroy", "fnum_pw_plan_set_sound_speed", "fnum_pw_sharpness_grad",
-    "fnum_plan_m_signal",
+    "fnum_plan_m_signal", "fnum_plan_set_kernel_variant",
 )
 
 ABI_VERSION = 3   # FNUM_ABI_VERSION of include/fnum.h
@@ -165,6 +165,8 @@ def lib():
                                       C.c_void_p]
     L.fnum_plan_autotune.restype = C.c_int
     L.fnum_plan_autotune.argtypes = [C.c_void_p, C.c_void_p, C.c_int, _ip, _fp]
+    L.fnum_plan_set_kernel_variant.restype = C.c_int
+    L.fnum_plan_set_kernel_variant.argtypes = [C.c_void_p, C.c_int]
     L.fnum_batch_create.restype = C.c_int
     L.fnum_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p), _ip,
                                     C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int,

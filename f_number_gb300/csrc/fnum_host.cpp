@@ -1144,6 +1144,17 @@ int fnum_das_sa(const fnum_sa_desc* desc, const double* data_rf, int flags, floa
 // autotuning and batches (no counterpart in the reference, which beamforms one
 // angle per gateway call)
 // ---------------------------------------------------------------------------
+int fnum_plan_set_kernel_variant(fnum_plan* plan, int variant) {
+  if (!plan) return FNUM_ERR_ARGUMENT;
+  if (plan->kind != 0) return variant == 0 ? FNUM_OK : FNUM_ERR_ARGUMENT;  // one synthetic-aperture variant
+  if (variant < 0 || variant > fnum::pw_variant_count()) return FNUM_ERR_ARGUMENT;
+  if (plan->pw.m_sem) return variant == 0 ? FNUM_OK : FNUM_ERR_ARGUMENT;     // one per-term kernel
+  FNUM_CUDA(cudaSetDevice(plan->device));
+  plan->pw.variant = variant;
+  plan->grid = std::min(fnum::pw_fused_grid(plan->pw, nullptr), plan->max_grid);
+  return FNUM_OK;
+}
+
 int fnum_plan_autotune(fnum_plan* plan, const void* d_rf, int rf_is_double, int* variant, float* ms) {
   if (!plan || !d_rf) return FNUM_ERR_ARGUMENT;
   FNUM_CUDA(cudaSetDevice(plan->device));

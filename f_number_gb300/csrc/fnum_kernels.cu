@@ -725,6 +725,258 @@ pw_fused_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
   if (tid == 0) atomicAdd(&d.counters[4], n_exec);
 }
 
+// Plane-wave recurrence with the segment boundaries resolved ahead of the bin
+// loop.  Each lane walks its own boundaries of the next EVB bins and writes,
+// per bin that carries one and per element of the pass, one value into a
+// table in shared memory (a column per lane):
+//   v > 0   the element stays in the aperture: rescale its accumulators by v
+//   v == 0  it enters the aperture (or stays out): clear them
+//   v < 0   it leaves the aperture: flush them with the weight -v, then clear
+// plus a bit mask of the bins that carry a boundary.  The bin loop applies a
+// table entry only where this lane has one, so a warp spends per bin of a
+// boundary a load and a multiply instead of the window evaluation.  The
+// arithmetic is that of pw_fused_kernel, which gives the same images.
+template <int EPT, int NA, int WIN>
+__global__ void __launch_bounds__(NTHREADS, 4)
+pw_event_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weights, int n_tiles_x,
+                int n_tiles_z) {
+  constexpr int CH = EPT * NA;
+  constexpr int ROW = (CH + 1) & ~1;
+  constexpr int EVB = (EPT <= 2) ? 32 : 16;   // bins per boundary table
+  __shared__ __align__(16) float2 xs[2][KCHUNK * ROW];
+  __shared__ dfl utx_s[NA][NTHREADS];
+  __shared__ float ev[EVB][EPT][NTHREADS];
+  __shared__ int e_range[2];
+  __shared__ int s_tile;
+  extern __shared__ __align__(16) unsigned char dyn[];  // lb[ne], ub[ne] (dfl), ktop[ne]
+  dfl* lb_s = (dfl*)dyn;
+  dfl* ub_s = lb_s + d.ne;
+  int* ktop = (int*)(ub_s + d.ne);
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int n_tiles = n_tiles_x * n_tiles_z;
+  int4* seg = d.seg + ((size_t)blockIdx.x * NTHREADS + tid) * (size_t)d.seg_cap * PW_SEG_INT4;
+  const float inv_par = (d.window_par > 0.0f) ? 1.0f / d.window_par : 0.0f;
+  unsigned long long n_active = 0, n_empty = 0, n_exec = 0;
+  for (int e = tid; e < d.ne; e += NTHREADS) {
+    lb_s[e] = d.el_lb[e];
+    ub_s[e] = d.el_ub[e];
+  }
+
+  for (;;) {
+    if (tid == 0) s_tile = (int)atomicAdd(&d.counters[3], 1ull);
+    for (int e = tid; e < d.ne; e += NTHREADS) ktop[e] = -1;
+    if (tid == 0) {
+      e_range[0] = d.ne;
+      e_range[1] = -1;
+    }
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= n_tiles) break;
+    int tx, tz;
+    tile_coords(tile, n_tiles_x, n_tiles_z, tx, tz);
+    const int i = tx * TILE_X + warp;
+    const int j = tz * TILE_Z + lane;
+    const bool valid = (i < d.nx) && (j < d.nz);
+    const int ic = min(i, d.nx - 1), jc = min(j, d.nz - 1);
+
+    float W_top;
+    const int nseg = pw_build_segments<WIN>(d, inv_par, ic, jc, valid, seg, ktop, e_range, W_top, n_active, n_empty);
+    __syncthreads();
+    const int E_lo = e_range[0], E_hi = e_range[1];
+
+    const dfl xm = d.col_m[ic];
+    const dfl xu = d.col_u[ic];
+    const dfl zu2 = d.row_u2[jc];
+    const int emid = d.col_emid[ic];
+    float2 acc = make_float2(0.0f, 0.0f), comp = make_float2(0.0f, 0.0f);  // Kahan
+
+    for (int a0 = 0; a0 < d.na; a0 += NA) {
+#pragma unroll
+      for (int a = 0; a < NA; ++a) {
+        const int aa = min(a0 + a, d.na - 1);
+        utx_s[a][tid] = df_add(d.tx_ax[(size_t)aa * d.nx + ic], d.tx_az[(size_t)aa * d.nz + jc]);
+      }
+      for (int e0 = E_lo; e0 <= E_hi; e0 += EPT) {
+        int kt = -1;
+#pragma unroll
+        for (int q = 0; q < EPT; ++q)
+          if (e0 + q <= E_hi) kt = max(kt, ktop[e0 + q]);
+        if (kt < d.k_lb) continue;
+        if (tid == 0) n_exec += (unsigned long long)(kt - d.k_lb + 1) * CH * NTHREADS;
+
+        // pre-pass state: element distance, window value and weight b = a / W
+        float dxa[EPT], aw[EPT], b[EPT];
+        dfl urx[EPT];
+        float2 z[EPT][NA], A[EPT][NA];
+#pragma unroll
+        for (int q = 0; q < EPT; ++q) {
+          const int e = min(e0 + q, d.ne - 1);
+          const dfl cm = d.el_m[e];
+          dxa[q] = fabsf((cm.x - xm.x) + (cm.y - xm.y));
+          urx[q] = df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2));
+#pragma unroll
+          for (int a = 0; a < NA; ++a) {
+            z[q][a] = cis_ku(1, df_add(urx[q], utx_s[a][tid]));
+            A[q][a] = make_float2(0.0f, 0.0f);
+          }
+        }
+        int s = 0, code = seg_code(d.ne, -1);
+        int4 ring[SEG_RING];
+#pragma unroll
+        for (int r = 0; r < SEG_RING; ++r) ring[r] = make_int4(-1, code, 0, 0);
+        if (nseg > 0) {
+          s = seg_find1(seg, nseg, kt);
+          const int4 c0 = seg[s];
+          code = c0.y;
+          const int ilb = code_ilb(code), iub = code_iub(code);
+          const int lo = min(ilb, emid), hi = max(iub, emid - 1);
+          const float invW = __int_as_float(c0.z);
+#pragma unroll
+          for (int q = 0; q < EPT; ++q) {
+            const int e = e0 + q;
+            const bool left = e < emid;
+            const bool act = (e >= lo) && (e <= hi) && (e <= E_hi);
+            aw[q] = act ? win_t<WIN>(d.window_par, inv_par,
+                                     dxa[q] * inv_half_width(lb_s, ub_s, xm, left, ilb, iub))
+                        : 0.0f;
+            b[q] = aw[q] * invW;
+          }
+#pragma unroll
+          for (int r = 0; r < SEG_RING; ++r) ring[r] = seg[min(s + 1 + r, nseg)];
+        } else {
+#pragma unroll
+          for (int q = 0; q < EPT; ++q) aw[q] = b[q] = 0.0f;
+        }
+        float2 part = make_float2(0.0f, 0.0f);
+
+        const int c_top = (kt - d.k_lb) / KCHUNK;
+        __syncthreads();  // every thread is done with both buffers of the previous pass
+        pw_stage_chunk<EPT, NA>(xs[0], d, e0, a0, d.k_lb + c_top * KCHUNK, kt - (d.k_lb + c_top * KCHUNK) + 1, tid);
+        int buf = 0;
+        for (int chunk = c_top; chunk >= 0; --chunk) {
+          const int kc_lo = d.k_lb + chunk * KCHUNK;
+          const int kc_hi = (chunk == c_top) ? kt : kc_lo + KCHUNK - 1;
+          cp_async_wait_all();
+          __syncthreads();  // the chunk is visible; the other buffer is free
+          if (chunk > 0) pw_stage_chunk<EPT, NA>(xs[buf ^ 1], d, e0, a0, kc_lo - KCHUNK, KCHUNK, tid);
+          const float2* xb = xs[buf];
+          buf ^= 1;
+          for (int ks_hi = kc_hi; ks_hi >= kc_lo; ks_hi -= EVB) {
+            const int ks_lo = max(kc_lo, ks_hi - (EVB - 1));
+            // this lane's boundaries in bins ks_lo .. ks_hi (the sentinel's bin -1 ends the walk)
+            unsigned emask = 0u;
+            while (ring[0].x >= ks_lo) {
+              const int kb = ring[0].x;
+              const int pilb = code_ilb(code), piub = code_iub(code);
+              code = ring[0].y;
+              const float invW = __int_as_float(ring[0].z), wr = __int_as_float(ring[0].w);
+#pragma unroll
+              for (int r = 0; r + 1 < SEG_RING; ++r) ring[r] = ring[r + 1];
+              ++s;
+              ring[SEG_RING - 1] = seg[min(s + SEG_RING, nseg)];
+              const int ilb = code_ilb(code), iub = code_iub(code);
+              const int lo = min(ilb, emid), hi = max(iub, emid - 1);
+#pragma unroll
+              for (int q = 0; q < EPT; ++q) {
+                const int e = e0 + q;
+                const bool left = e < emid;
+                const bool act = (e >= lo) && (e <= hi) && (e <= E_hi);
+                const float bo = b[q];
+                float r = wr;
+                if (act) {
+                  if ((left ? (ilb != pilb) : (iub != piub)) || bo == 0.0f) {
+                    const float an = win_t<WIN>(d.window_par, inv_par,
+                                              dxa[q] * inv_half_width(lb_s, ub_s, xm, left, ilb, iub));
+                    r = __fdividef(aw[q], an) * wr;
+                    aw[q] = an;
+                  }
+                } else {
+                  aw[q] = 0.0f;
+                }
+                const float bn = aw[q] * invW;
+                ev[kb - ks_lo][q][tid] = (bn != 0.0f && bo != 0.0f) ? r : ((bo != 0.0f) ? -bo : 0.0f);
+                b[q] = bn;
+              }
+              emask |= 1u << (kb - ks_lo);
+            }
+            int nev = emask ? ks_lo + 31 - __clz(emask) : -1;
+            for (int k = ks_hi; k >= ks_lo; --k) {
+              if (k == nev) {
+#pragma unroll
+                for (int q = 0; q < EPT; ++q) {
+                  const float v = ev[k - ks_lo][q][tid];
+                  if (v < 0.0f) {  // leaves the aperture below k+1: flush at k+1
+#pragma unroll
+                    for (int a = 0; a < NA; ++a) {
+                      const float2 t = cmul(cis_ku(k + 1, df_add(urx[q], utx_s[a][tid])), A[q][a]);
+                      part.x = fmaf(-v, t.x, part.x);
+                      part.y = fmaf(-v, t.y, part.y);
+                    }
+                  }
+                  const bool keep = v > 0.0f;
+#pragma unroll
+                  for (int a = 0; a < NA; ++a) {
+                    A[q][a].x = keep ? A[q][a].x * v : 0.0f;
+                    A[q][a].y = keep ? A[q][a].y * v : 0.0f;
+                  }
+                }
+                emask &= ~(1u << (k - ks_lo));
+                nev = emask ? ks_lo + 31 - __clz(emask) : -1;
+              }
+              const float2* xr = &xb[(k - kc_lo) * ROW];
+#pragma unroll
+              for (int q = 0; q < EPT; ++q) {
+#pragma unroll
+                for (int a = 0; a < NA; ++a) {
+                  const float2 x = xr[q * NA + a];
+                  const float2 Aq = A[q][a], zq = z[q][a];
+                  A[q][a].x = fmaf(Aq.x, zq.x, fmaf(-Aq.y, zq.y, x.x));
+                  A[q][a].y = fmaf(Aq.x, zq.y, fmaf(Aq.y, zq.x, x.y));
+                }
+              }
+            }
+          }
+          if (chunk % d.flush_chunks == 0) {
+#pragma unroll
+            for (int q = 0; q < EPT; ++q) {
+              if (b[q] != 0.0f) {
+#pragma unroll
+                for (int a = 0; a < NA; ++a) {
+                  const float2 t = cmul(cis_ku(kc_lo, df_add(urx[q], utx_s[a][tid])), A[q][a]);
+                  part.x = fmaf(b[q], t.x, part.x);
+                  part.y = fmaf(b[q], t.y, part.y);
+                }
+              }
+#pragma unroll
+              for (int a = 0; a < NA; ++a) A[q][a] = make_float2(0.0f, 0.0f);
+            }
+          }
+        }
+        {
+          float y = part.x - comp.x, t = acc.x + y;
+          comp.x = (t - acc.x) - y;
+          acc.x = t;
+          y = part.y - comp.y;
+          t = acc.y + y;
+          comp.y = (t - acc.y) - y;
+          acc.y = t;
+        }
+      }
+    }
+    if (valid) {
+      image[(size_t)ic * d.nz + jc] = make_float2(acc.x * d.scale, acc.y * d.scale);
+      if (weights) weights[(size_t)ic * d.nz + jc] = W_top;
+    }
+    __syncthreads();
+  }
+  n_active *= (unsigned long long)d.na;
+  n_empty *= (unsigned long long)d.na;
+  atomicAdd(&d.counters[0], n_active);
+  atomicAdd(&d.counters[1], n_empty);
+  if (tid == 0) atomicAdd(&d.counters[4], n_exec);
+}
+
 typedef void (*pw_kernel_t)(const PWDev, float2*, float*, int, int);
 
 template <int EPT, int NA>
@@ -736,16 +988,33 @@ static pw_kernel_t pw_pick_win(int window_id) {
     default: return pw_fused_kernel<EPT, NA, 4>;
   }
 }
+template <int EPT, int NA>
+static pw_kernel_t pw_pick_event_win(int window_id) {
+  switch (window_id) {
+    case 0: return pw_event_kernel<EPT, NA, 0>;
+    case 1: return pw_event_kernel<EPT, NA, 1>;
+    case 2: return pw_event_kernel<EPT, NA, 2>;
+    default: return pw_event_kernel<EPT, NA, 4>;
+  }
+}
 
-// Kernel variants: how many elements (EPT) and angles (NA) one pass carries.
-//   1: EPT 1 x NA 11   2: EPT 2 x NA 4   3: EPT 2 x NA 2   4: EPT 4 x NA 1
+// Kernel variants: how many elements (EPT) and angles (NA) one pass carries,
+// and where the segment boundaries are resolved.
+//   boundaries resolved ahead of the bin loop (pw_event_kernel):
+//     1: EPT 1 x NA 11   2: EPT 2 x NA 4   3: EPT 2 x NA 2   4: EPT 4 x NA 1
+//   boundaries resolved inside the bin loop (pw_fused_kernel):
+//     5: EPT 1 x NA 11   6: EPT 2 x NA 4   7: EPT 2 x NA 2   8: EPT 4 x NA 1
 // Angles beyond NA run as further passes inside the launch.  PWDev::variant
 // 0 picks by the angle count; a plan's autotuner may set another.
 static pw_kernel_t pw_variant_kernel(int v, int window_id) {
   switch (v) {
-    case 1: return pw_pick_win<1, 11>(window_id);
-    case 2: return pw_pick_win<2, 4>(window_id);
-    case 3: return pw_pick_win<2, 2>(window_id);
+    case 1: return pw_pick_event_win<1, 11>(window_id);
+    case 2: return pw_pick_event_win<2, 4>(window_id);
+    case 3: return pw_pick_event_win<2, 2>(window_id);
+    case 4: return pw_pick_event_win<4, 1>(window_id);
+    case 5: return pw_pick_win<1, 11>(window_id);
+    case 6: return pw_pick_win<2, 4>(window_id);
+    case 7: return pw_pick_win<2, 2>(window_id);
     default: return pw_pick_win<4, 1>(window_id);
   }
 }
@@ -758,7 +1027,7 @@ static int pw_default_variant(int na) {
 static pw_kernel_t pw_pick(const PWDev& d) {
   return pw_variant_kernel(d.variant > 0 ? d.variant : pw_default_variant(d.na), d.window_id);
 }
-int pw_variant_count() { return 4; }
+int pw_variant_count() { return 8; }
 int pw_variant_of(const PWDev& d) { return d.variant > 0 ? d.variant : pw_default_variant(d.na); }
 
 int pw_fused_grid(const PWDev& d, int* blocks_per_sm) {

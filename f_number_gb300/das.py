@@ -488,6 +488,11 @@ class _Plan:
                                                  _lib.C.byref(v), _lib.C.byref(ms)), self._saft)
         return v.value, ms.value
 
+    def set_kernel_variant(self, variant):
+        """Pins the fused kernel's variant (fnum_plan_set_kernel_variant): 0 = by the
+        angle count, 1..8 for a plane-wave plan."""
+        _lib.check(_lib.lib().fnum_plan_set_kernel_variant(self._ptr, int(variant)), self._saft)
+
 
 class PWPlan(_Plan):
     """Plane-wave plan: one or many steering angles with the same geometry."""
