@@ -145,8 +145,15 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def pw_kernel_name(variant, window):
+    """Name of the plane-wave fused kernel a plan's variant launches."""
+    shapes = {1: (1, 11), 2: (2, 4), 3: (2, 2), 4: (4, 1)}
+    ept, na = shapes[(variant - 1) % 4 + 1]
+    return "%s<%d,%d,%s>" % ("pw_event_kernel" if variant <= 4 else "pw_fused_kernel", ept, na, window)
+
+
 def traffic_from_profiles():
-    p = os.path.join(ROOT, "profiles", "pw_fused_cpwc_512.json")
+    p = os.path.join(ROOT, "profiles", "pw_event_cpwc_512.json")
     if os.path.exists(p):
         try:
             return json.load(open(p)).get("dram_bytes_per_launch")
@@ -277,7 +284,7 @@ def run_ours(args):
     achieved = flops / (bf_avg_ms * 1e-3) / 1e12
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
             "frac": achieved / peak.value if peak.value else None, "traffic": traffic_from_profiles(),
-            "kernel": "pw_plain_kernel" if args.kernel == "plain" else "pw_fused_kernel<1,11,hann>",
+            "kernel": "pw_plain_kernel" if args.kernel == "plain" else pw_kernel_name(info["kernel_variant"], "hann"),
             "work": "8 FLOP per active voxel x element x bin x angle term "
             "(complex MAC); %d active of %d nominal terms" % (info["active_terms"], info["terms"]),
             "executed_terms": info["executed_terms"],
@@ -362,7 +369,7 @@ def run_saft(args):
     achieved = 8.0 * active / (bf_ms * 1e-3) / 1e12
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
             "frac": achieved / peak.value if peak.value else None, "traffic": None,
-            "kernel": "sa_fused_kernel<8>" if args.kernel == "fused" else "sa_plain_kernel",
+            "kernel": "sa_event_kernel<12,boxcar> (boxcar receive window)" if args.kernel == "fused" else "sa_plain_kernel",
             "work": "8 FLOP per active voxel x tx x rx x bin term; %d active of %d nominal terms"
             % (info["active_terms"], info["terms"]),
             "peak_source": "measured FP32 FMA throughput (fnum_diag_fp32_peak)"}

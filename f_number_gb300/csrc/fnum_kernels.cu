@@ -1719,13 +1719,14 @@ sa_event_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
   }
 }
 
-constexpr int SA_EPT = 8;
+constexpr int SA_EPT = 8;      // receive chains per pass, boundaries resolved in the bin loop
+constexpr int SA_EV_EPT = 12;  // receive chains per pass of sa_event_kernel
 typedef void (*sa_kernel_t)(const SADev, float2*, float*, float*, int, int, int);
 
 template <int WT>
 static sa_kernel_t sa_pick_rx(int wr) {
   switch (wr) {
-    case 0: return sa_event_kernel<SA_EPT, WT>;   // boxcar receive window
+    case 0: return sa_event_kernel<SA_EV_EPT, WT>;   // boxcar receive window
     case 1: return sa_fused_kernel<SA_EPT, WT, 1>;
     case 2: return sa_fused_kernel<SA_EPT, WT, 2>;
     default: return sa_fused_kernel<SA_EPT, WT, 4>;
