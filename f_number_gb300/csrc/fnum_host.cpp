@@ -706,6 +706,12 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
     D.seg = seg;
     P->info.scratch_bytes =
         (long long)P->max_grid * fnum::NTHREADS * D.seg_cap * fnum::PW_SEG_INT4 * (long long)sizeof(int4);
+    // tensor-core variant: spectra as mma fragments (96 uint4 per bin and group of 8 elements)
+    D.tc_S = (ne + 7) / 8 + 1;
+    const size_t n_tc = (size_t)((na + fnum::TC_NA - 1) / fnum::TC_NA) * D.K * D.tc_S * 96;
+    if ((s = P->alloc(&D.tc_B, n_tc))) goto fail;
+    if ((s = P->alloc(&D.tc_max, 1))) goto fail;
+    P->info.scratch_bytes += (long long)(n_tc * sizeof(uint4) + sizeof(unsigned));
   }
   {
     cudaError_t e = fnum::launch_twiddles(P->tw, b.N, 0);
@@ -1148,6 +1154,7 @@ int fnum_plan_set_kernel_variant(fnum_plan* plan, int variant) {
   if (!plan) return FNUM_ERR_ARGUMENT;
   if (plan->kind != 0) return variant == 0 ? FNUM_OK : FNUM_ERR_ARGUMENT;  // one synthetic-aperture variant
   if (variant < 0 || variant > fnum::pw_variant_count()) return FNUM_ERR_ARGUMENT;
+  if (variant == fnum::TC_VARIANT && !plan->pw.tc_B) return FNUM_ERR_ARGUMENT;
   if (plan->pw.m_sem) return variant == 0 ? FNUM_OK : FNUM_ERR_ARGUMENT;     // one per-term kernel
   FNUM_CUDA(cudaSetDevice(plan->device));
   plan->pw.variant = variant;

@@ -16,6 +16,10 @@ constexpr int TILE_Z = 32;
 constexpr int NTHREADS = TILE_X * TILE_Z;
 // band bins per shared-memory spectrum chunk; flushes happen on chunk edges
 constexpr int KCHUNK = 64;
+// tensor-core plane-wave kernel: 4 warps of 16 voxels, TC_TILE_X columns x TILE_Z rows
+constexpr int TC_TILE_X = 2;
+constexpr int TC_NA = 12;   // angles per angle pass (3 mma n-tiles of 4 complex angles)
+constexpr int TC_VARIANT = 9;
 
 // one aperture segment of one voxel (bins k_start down to the next entry's
 // k_start + 1 share the same apertures).  Plane wave: one int4
@@ -57,6 +61,11 @@ struct PWDev {
   int x_na, x_a0;
   // scratch: [grid][NTHREADS][seg_cap] int4
   int4* seg;
+  // tensor-core variant: spectra as mma B fragments [angle pass][K][tc_S][3][32] (uint4),
+  // and the largest |component| of the spectra (float bits) that sets their fp16 scale
+  uint4* tc_B;
+  unsigned* tc_max;
+  int tc_S;            // element groups of 8 in tc_B (one zero group of padding included)
   unsigned long long* counters;   // [0] active terms, [1] zero-weight bins, [2] error bits,
                                   // [3] tile counter, [4] executed recurrence steps
   // the per-voxel FP32 kernel reads the reference's float geometry

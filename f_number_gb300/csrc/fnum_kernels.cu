@@ -30,6 +30,7 @@
 // in shared memory with cp.async so the next chunk loads during the current one.
 #include "fnum_internal.h"
 
+#include <cuda_fp16.h>
 #include <float.h>
 #include <math.h>
 #include <stdint.h>
@@ -977,6 +978,376 @@ pw_event_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
   if (tid == 0) atomicAdd(&d.counters[4], n_exec);
 }
 
+// ---------------------------------------------------------------------------
+// plane-wave kernel on the tensor cores
+// ---------------------------------------------------------------------------
+// Per bin k the compounded image gains
+//   sum_a t_{v,a}^k G_k(v, a),   G_k(v, a) = sum_e R_k(v, e) X_k(e, a),
+//   R_k(v, e) = b_{v,e,k} r_{v,e}^k,
+// with r = e^{j 2 pi u_rx}, t = e^{j 2 pi u_tx} and b the apodization weight
+// a / W.  G_k is a [voxels x elements] . [elements x angles] product per bin,
+// run with warp-level mma.sync m16n8k16 (fp16 operands, fp32 accumulators) in
+// real form,
+//   [Rr Ri] . [[Xr Xi], [-Xi Xr]] = [Gr Gi],
+// 16 voxels x 8 complex elements x 4 complex angles per instruction.  Each
+// fp32 operand is split into fp16 hi + lo (the spectra scaled by a power of
+// two into fp16 range) and hi.hi + hi.lo + lo.hi is accumulated, which keeps
+// about 22 bits.  The transmit phases are applied by a Horner recurrence over
+// bins per (voxel, angle) inside the accumulators, H <- H t + G_k, flushed with
+// the exact phase at the end of every TC_TB bins, where the receive phasors
+// r^k are also re-anchored exactly.  The weights b enter R bin by bin, so a
+// segment boundary costs nothing in the recurrence: the per-(voxel, bin)
+// aperture data come from the segment lists through a table in shared memory
+// that lanes 0..15 of each warp fill ahead of the bins.
+constexpr int TC_WARPS = NTHREADS / 32;
+constexpr int TC_EP = 16;   // elements per pass (two mma k-steps of 8 complex elements)
+constexpr int TC_TB = 32;   // bins per aperture table and per flush
+
+__device__ __forceinline__ void tc_split(float x0, float x1, unsigned& hi, unsigned& lo) {
+  const __half2 h = __floats2half2_rn(x0, x1);
+  const float2 f = __half22float2(h);
+  const __half2 l = __floats2half2_rn(x0 - f.x, x1 - f.y);
+  hi = *reinterpret_cast<const unsigned*>(&h);
+  lo = *reinterpret_cast<const unsigned*>(&l);
+}
+
+// D += A B for one m16n8k16 tile (row-major A, column-major B, fp32 accumulators)
+__device__ __forceinline__ void tc_mma(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// largest |component| of the band spectra of the launch's angles (float bits; >= 0 floats order as ints)
+__global__ void __launch_bounds__(256) tc_absmax_kernel(const PWDev d, unsigned* out) {
+  const size_t n = (size_t)d.ne * d.K * d.na;
+  float m = 0.0f;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t a = i % d.na, ek = i / d.na;
+    const float2 x = d.X[ek * d.x_na + d.x_a0 + a];
+    m = fmaxf(m, fmaxf(fabsf(x.x), fabsf(x.y)));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+// power-of-two scale that brings the spectra below 2^14 (exact in both directions)
+__device__ __forceinline__ float tc_scale(unsigned maxbits) {
+  const float m = __uint_as_float(maxbits);
+  if (!(m > 0.0f) || !(m < 3.0e38f)) return 1.0f;
+  int ex;
+  frexpf(m, &ex);  // m < 2^ex
+  return ldexpf(1.0f, min(max(14 - ex, -126), 126));
+}
+
+// B fragments of the spectra: for angle pass ap, bin kk, element group s (elements
+// 8s .. 8s+7), n-tile j (angles ap*TC_NA + 4j .. +3) and lane (g = lane/4, q = lane%4):
+//   b0 = {B[2q][g], B[2q+1][g]}, b1 = {B[2q+8][g], B[2q+9][g]} as fp16 hi, then lo,
+// with rows 0..7 the Rr rows and 8..15 the Ri rows of the group's elements and
+// column g = 2 (angle) + (0: Gr, 1: Gi).
+__global__ void __launch_bounds__(256) tc_prep_kernel(const PWDev d, int n_ap) {
+  const size_t n = (size_t)n_ap * d.K * d.tc_S * 3 * 32;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float sigma = tc_scale(*d.tc_max);
+  const int lane = (int)(i & 31);
+  size_t r = i >> 5;
+  const int j = (int)(r % 3);
+  r /= 3;
+  const int s = (int)(r % d.tc_S);
+  r /= d.tc_S;
+  const int kk = (int)(r % d.K);
+  const int ap = (int)(r / d.K);
+  const int g = lane >> 2, q = lane & 3;
+  const int a = ap * TC_NA + 4 * j + (g >> 1), part = g & 1;
+  float rr[2], ri[2];
+#pragma unroll
+  for (int t = 0; t < 2; ++t) {
+    const int e = 8 * s + 2 * q + t;
+    float2 x = make_float2(0.0f, 0.0f);
+    if (e < d.ne && a < d.na) x = d.X[((size_t)e * d.K + kk) * d.x_na + d.x_a0 + a];
+    x.x *= sigma;
+    x.y *= sigma;
+    rr[t] = part ? x.y : x.x;
+    ri[t] = part ? x.x : -x.y;
+  }
+  uint4 o;
+  tc_split(rr[0], rr[1], o.x, o.z);
+  tc_split(ri[0], ri[1], o.y, o.w);
+  d.tc_B[i] = o;
+}
+
+template <int WIN>
+__global__ void __launch_bounds__(NTHREADS, 4)
+pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weights, int n_tiles_x, int n_tiles_z) {
+  __shared__ float4 apt[TC_WARPS][TC_TB][16];   // {lo | (hi+1) << 16, 1/L_left, 1/L_right, 1/W} per bin, voxel
+  __shared__ int e_range[2];
+  __shared__ int s_tile;
+  __shared__ int s_nseg[TC_WARPS * 16];
+  // table builders' state (entry in effect, next segment entry, its index) and the
+  // threads' compensated sums per voxel, kept out of registers
+  __shared__ float4 b_ent[TC_WARPS * 16];
+  __shared__ int4 b_next[TC_WARPS * 16];
+  __shared__ int b_idx[TC_WARPS * 16];
+  __shared__ float4 s_acc[2][NTHREADS];   // {acc.x, acc.y, comp.x, comp.y} per voxel V
+  extern __shared__ __align__(16) unsigned char dyn[];  // lb[ne], ub[ne] (dfl), ktop[ne]
+  dfl* lb_s = (dfl*)dyn;
+  dfl* ub_s = lb_s + d.ne;
+  int* ktop = (int*)(ub_s + d.ne);
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, q = lane & 3;
+  const int n_tiles = n_tiles_x * n_tiles_z;
+  int4* seg_blk = d.seg + (size_t)blockIdx.x * NTHREADS * (size_t)d.seg_cap * PW_SEG_INT4;
+  const float inv_par = (d.window_par > 0.0f) ? 1.0f / d.window_par : 0.0f;
+  const float inv_sigma = 1.0f / tc_scale(*d.tc_max);
+  unsigned long long n_active = 0, n_empty = 0, n_exec = 0;
+  for (int e = tid; e < d.ne; e += NTHREADS) {
+    lb_s[e] = d.el_lb[e];
+    ub_s[e] = d.el_ub[e];
+  }
+
+  for (;;) {
+    if (tid == 0) s_tile = (int)atomicAdd(&d.counters[3], 1ull);
+    for (int e = tid; e < d.ne; e += NTHREADS) ktop[e] = -1;
+    if (tid == 0) {
+      e_range[0] = d.ne;
+      e_range[1] = -1;
+    }
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= n_tiles) break;
+    int tx, tz;
+    tile_coords(tile, n_tiles_x, n_tiles_z, tx, tz);
+    // block voxel vb (0..63): column vb / 32, row vb % 32; threads 0..63 build its segment list
+    if (tid < TC_WARPS * 16) {
+      const int i = tx * TC_TILE_X + (tid >> 5), j = tz * TILE_Z + (tid & 31);
+      const bool valid = (i < d.nx) && (j < d.nz);
+      const int ic = min(i, d.nx - 1), jc = min(j, d.nz - 1);
+      float W_top;
+      s_nseg[tid] = pw_build_segments<WIN>(d, inv_par, ic, jc, valid, seg_blk + (size_t)tid * d.seg_cap, ktop,
+                                           e_range, W_top, n_active, n_empty);
+      if (valid && weights) weights[(size_t)ic * d.nz + jc] = W_top;
+    }
+    __syncthreads();
+    const int E_lo = e_range[0] & ~7, E_hi = e_range[1];
+
+    // the thread's voxels: mma rows g and g + 8 of its warp
+    int vic[2], vjc[2], emid[2];
+    bool vvalid[2];
+#pragma unroll
+    for (int V = 0; V < 2; ++V) {
+      const int vb = 16 * warp + g + 8 * V;
+      const int i = tx * TC_TILE_X + (vb >> 5), j = tz * TILE_Z + (vb & 31);
+      vvalid[V] = (i < d.nx) && (j < d.nz);
+      vic[V] = min(i, d.nx - 1);
+      vjc[V] = min(j, d.nz - 1);
+      emid[V] = d.col_emid[vic[V]];
+    }
+    // table builder: lane l < 16 serves voxel 16 * warp + l
+    const int bv = 16 * warp + (lane & 15);
+    const int4* bseg = seg_blk + (size_t)bv * d.seg_cap;
+    const int bnseg = s_nseg[bv];
+    const dfl bxm = d.col_m[min(tx * TC_TILE_X + (bv >> 5), d.nx - 1)];
+    const int bemid = d.col_emid[min(tx * TC_TILE_X + (bv >> 5), d.nx - 1)];
+    auto entry_of = [&](int4 c) -> float4 {
+      const int ilb = code_ilb(c.y), iub = code_iub(c.y);
+      const int lo = min(ilb, bemid), hi = max(iub, bemid - 1);
+      float il = 0.0f, ir = 0.0f;
+      if (ilb < d.ne) {
+        const dfl l = lb_s[ilb];
+        il = __fdividef(1.0f, (bxm.x - l.x) + (bxm.y - l.y));
+      }
+      if (iub >= 0) {
+        const dfl u = ub_s[iub];
+        ir = __fdividef(1.0f, (u.x - bxm.x) + (u.y - bxm.y));
+      }
+      return make_float4(__int_as_float(lo | ((hi + 1) << 16)), il, ir, __int_as_float(c.z));
+    };
+    s_acc[0][tid] = s_acc[1][tid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+
+    for (int a0 = 0; a0 < d.na; a0 += TC_NA) {
+      float2 tph[2][3];   // transmit phasor of (voxel V, angle a0 + 4j + q)
+#pragma unroll
+      for (int V = 0; V < 2; ++V)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const int aa = min(a0 + 4 * j + q, d.na - 1);
+          tph[V][j] = cis_ku(1, df_add(d.tx_ax[(size_t)aa * d.nx + vic[V]], d.tx_az[(size_t)aa * d.nz + vjc[V]]));
+        }
+      const uint4* Bp = d.tc_B + (size_t)(a0 / TC_NA) * d.K * d.tc_S * 96;
+      for (int e0 = E_lo; e0 <= E_hi; e0 += TC_EP) {
+        int kt = -1;
+        for (int e = max(e0, 0); e < min(e0 + TC_EP, E_hi + 1); ++e) kt = max(kt, ktop[e]);
+        if (kt < d.k_lb) continue;
+        if (tid == 0)
+          n_exec += (unsigned long long)(kt - d.k_lb + 1) * TC_EP * min(TC_NA, d.na - a0) * (TC_WARPS * 16);
+        // the thread's (voxel, element) pairs: V, element e0 + 8s + 2q + i
+        float dxa[2][2][2];
+        float2 cr[2][2][2], p[2][2][2];
+#pragma unroll
+        for (int V = 0; V < 2; ++V) {
+          const dfl xm = d.col_m[vic[V]], xu = d.col_u[vic[V]], zu2 = d.row_u2[vjc[V]];
+#pragma unroll
+          for (int s = 0; s < 2; ++s)
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+              const int e = min(e0 + 8 * s + 2 * q + i, d.ne - 1);
+              const dfl cm = d.el_m[e];
+              dxa[V][s][i] = fabsf((cm.x - xm.x) + (cm.y - xm.y));
+              const float2 r = cis_ku(1, df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2)));
+              cr[V][s][i] = make_float2(r.x, -r.y);
+            }
+        }
+        float H[3][4];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) H[j][0] = H[j][1] = H[j][2] = H[j][3] = 0.0f;
+        // builder state: the segment in effect and the next entry
+        if (lane < 16) {
+          int bs = 0;
+          float4 bent = make_float4(__int_as_float(d.ne), 0.0f, 0.0f, 0.0f);  // lo = ne, hi = -1: empty
+          int4 bnext = make_int4(-1, 0, 0, 0);
+          if (bnseg > 0) {
+            bs = seg_find1(bseg, bnseg, kt);
+            bent = entry_of(bseg[bs]);
+            bnext = bseg[min(bs + 1, bnseg)];
+          }
+          b_ent[bv] = bent;
+          b_next[bv] = bnext;
+          b_idx[bv] = bs;
+        }
+        const uint4* Bpe = Bp + (size_t)(e0 >> 3) * 96 + lane;
+        for (int kc_hi = kt; kc_hi >= d.k_lb; kc_hi -= TC_TB) {
+          const int kc_lo = max(d.k_lb, kc_hi - (TC_TB - 1));
+          __syncwarp();
+          if (lane < 16) {
+            int bs = b_idx[bv];
+            float4 bent = b_ent[bv];
+            int4 bnext = b_next[bv];
+            for (int k = kc_hi; k >= kc_lo; --k) {
+              if (k == bnext.x) {
+                bent = entry_of(bnext);
+                ++bs;
+                bnext = bseg[min(bs + 1, bnseg)];
+              }
+              apt[warp][kc_hi - k][lane] = bent;
+            }
+            b_ent[bv] = bent;
+            b_next[bv] = bnext;
+            b_idx[bv] = bs;
+          }
+          // receive phasors re-anchored exactly at the chunk's first bin
+#pragma unroll
+          for (int V = 0; V < 2; ++V) {
+            const dfl xu = d.col_u[vic[V]], zu2 = d.row_u2[vjc[V]];
+#pragma unroll
+            for (int s = 0; s < 2; ++s)
+#pragma unroll
+              for (int i = 0; i < 2; ++i) {
+                const int e = min(e0 + 8 * s + 2 * q + i, d.ne - 1);
+                p[V][s][i] = cis_ku(kc_hi, df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2)));
+              }
+          }
+          __syncwarp();
+          for (int k = kc_hi; k >= kc_lo; --k) {
+            float4 en[2];
+            en[0] = apt[warp][kc_hi - k][g];
+            en[1] = apt[warp][kc_hi - k][g + 8];
+            // H <- H t
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+#pragma unroll
+              for (int V = 0; V < 2; ++V) {
+                const float hr = H[j][2 * V], hi = H[j][2 * V + 1];
+                const float2 t = tph[V][j];
+                H[j][2 * V] = fmaf(hr, t.x, -hi * t.y);
+                H[j][2 * V + 1] = fmaf(hr, t.y, hi * t.x);
+              }
+            const uint4* Bk = Bpe + (size_t)(k - d.k_lb) * d.tc_S * 96;
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+              uint4 bf[3];
+#pragma unroll
+              for (int j = 0; j < 3; ++j) bf[j] = __ldg(Bk + s * 96 + j * 32);
+              float rre[2][2], rim[2][2];
+#pragma unroll
+              for (int V = 0; V < 2; ++V) {
+                const int lohi = __float_as_int(en[V].x);
+                const int lo = lohi & 0xffff, hi = (lohi >> 16) - 1;
+#pragma unroll
+                for (int i = 0; i < 2; ++i) {
+                  const int e = e0 + 8 * s + 2 * q + i;
+                  const float invL = (e < emid[V]) ? en[V].y : en[V].z;
+                  const float w = win_t<WIN>(d.window_par, inv_par, dxa[V][s][i] * invL);
+                  const float b = (e >= lo && e <= hi) ? w * en[V].w : 0.0f;
+                  const float2 pp = p[V][s][i];
+                  rre[V][i] = b * pp.x;
+                  rim[V][i] = b * pp.y;
+                  p[V][s][i] = cmul(pp, cr[V][s][i]);
+                }
+              }
+              unsigned ah[4], al[4];
+              tc_split(rre[0][0], rre[0][1], ah[0], al[0]);
+              tc_split(rre[1][0], rre[1][1], ah[1], al[1]);
+              tc_split(rim[0][0], rim[0][1], ah[2], al[2]);
+              tc_split(rim[1][0], rim[1][1], ah[3], al[3]);
+#pragma unroll
+              for (int j = 0; j < 3; ++j) {
+                tc_mma(H[j], ah, bf[j].x, bf[j].y);
+                tc_mma(H[j], ah, bf[j].z, bf[j].w);
+                tc_mma(H[j], al, bf[j].x, bf[j].y);
+              }
+            }
+          }
+          // flush: the image gains t^{kc_lo} H with the exact phase
+#pragma unroll
+          for (int V = 0; V < 2; ++V) {
+            float2 part = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+              const int a = a0 + 4 * j + q;
+              if (a < d.na) {
+                const float2 c = cis_ku(kc_lo, df_add(d.tx_ax[(size_t)a * d.nx + vic[V]],
+                                                      d.tx_az[(size_t)a * d.nz + vjc[V]]));
+                const float2 t = cmul(c, make_float2(H[j][2 * V], H[j][2 * V + 1]));
+                part.x += t.x;
+                part.y += t.y;
+              }
+              H[j][2 * V] = H[j][2 * V + 1] = 0.0f;
+            }
+            float4 a4 = s_acc[V][tid];
+            float y = part.x - a4.z, t = a4.x + y;
+            a4.z = (t - a4.x) - y;
+            a4.x = t;
+            y = part.y - a4.w;
+            t = a4.y + y;
+            a4.w = (t - a4.y) - y;
+            a4.y = t;
+            s_acc[V][tid] = a4;
+          }
+        }
+      }
+    }
+    // the four lanes of a group hold the voxel's sums over their angles
+#pragma unroll
+    for (int V = 0; V < 2; ++V) {
+      float x = s_acc[V][tid].x, y = s_acc[V][tid].y;
+      x += __shfl_xor_sync(0xffffffffu, x, 1);
+      y += __shfl_xor_sync(0xffffffffu, y, 1);
+      x += __shfl_xor_sync(0xffffffffu, x, 2);
+      y += __shfl_xor_sync(0xffffffffu, y, 2);
+      if (q == 0 && vvalid[V])
+        image[(size_t)vic[V] * d.nz + vjc[V]] = make_float2(x * d.scale * inv_sigma, y * d.scale * inv_sigma);
+    }
+    __syncthreads();
+  }
+  n_active *= (unsigned long long)d.na;
+  n_empty *= (unsigned long long)d.na;
+  atomicAdd(&d.counters[0], n_active);
+  atomicAdd(&d.counters[1], n_empty);
+  if (tid == 0) atomicAdd(&d.counters[4], n_exec);
+}
+
 typedef void (*pw_kernel_t)(const PWDev, float2*, float*, int, int);
 
 template <int EPT, int NA>
@@ -1004,10 +1375,21 @@ static pw_kernel_t pw_pick_event_win(int window_id) {
 //     1: EPT 1 x NA 11   2: EPT 2 x NA 4   3: EPT 2 x NA 2   4: EPT 4 x NA 1
 //   boundaries resolved inside the bin loop (pw_fused_kernel):
 //     5: EPT 1 x NA 11   6: EPT 2 x NA 4   7: EPT 2 x NA 2   8: EPT 4 x NA 1
+//   9: tensor cores (pw_tc_kernel), 16 elements x 12 angles per pass; needs
+//      the plan's fragment scratch (PWDev::tc_B)
 // Angles beyond NA run as further passes inside the launch.  PWDev::variant
 // 0 picks by the angle count; a plan's autotuner may set another.
+static pw_kernel_t pw_pick_tc_win(int window_id) {
+  switch (window_id) {
+    case 0: return pw_tc_kernel<0>;
+    case 1: return pw_tc_kernel<1>;
+    case 2: return pw_tc_kernel<2>;
+    default: return pw_tc_kernel<4>;
+  }
+}
 static pw_kernel_t pw_variant_kernel(int v, int window_id) {
   switch (v) {
+    case TC_VARIANT: return pw_pick_tc_win(window_id);
     case 1: return pw_pick_event_win<1, 11>(window_id);
     case 2: return pw_pick_event_win<2, 4>(window_id);
     case 3: return pw_pick_event_win<2, 2>(window_id);
@@ -1027,8 +1409,13 @@ static int pw_default_variant(int na) {
 static pw_kernel_t pw_pick(const PWDev& d) {
   return pw_variant_kernel(d.variant > 0 ? d.variant : pw_default_variant(d.na), d.window_id);
 }
-int pw_variant_count() { return 8; }
+int pw_variant_count() { return 9; }
 int pw_variant_of(const PWDev& d) { return d.variant > 0 ? d.variant : pw_default_variant(d.na); }
+
+static int pw_tiles_x(const PWDev& d) {
+  const int tw = pw_variant_of(d) == TC_VARIANT ? TC_TILE_X : TILE_X;
+  return (d.nx + tw - 1) / tw;
+}
 
 int pw_fused_grid(const PWDev& d, int* blocks_per_sm) {
   pw_kernel_t fn = pw_pick(d);
@@ -1038,7 +1425,7 @@ int pw_fused_grid(const PWDev& d, int* blocks_per_sm) {
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, NTHREADS, (size_t)d.ne * (sizeof(int) + 2 * sizeof(dfl)));
   if (bps < 1) bps = 1;
   if (blocks_per_sm) *blocks_per_sm = bps;
-  const int tiles = ((d.nx + TILE_X - 1) / TILE_X) * ((d.nz + TILE_Z - 1) / TILE_Z);
+  const int tiles = pw_tiles_x(d) * ((d.nz + TILE_Z - 1) / TILE_Z);
   return tiles < nsm * bps ? tiles : nsm * bps;
 }
 
@@ -1053,11 +1440,21 @@ int pw_fused_max_grid(const PWDev& d) {
 }
 
 cudaError_t launch_pw_fused(const PWDev& d, int grid, float2* image, float* weights, cudaStream_t s) {
-  const int ntx = (d.nx + TILE_X - 1) / TILE_X, ntz = (d.nz + TILE_Z - 1) / TILE_Z;
+  const int ntx = pw_tiles_x(d), ntz = (d.nz + TILE_Z - 1) / TILE_Z;
   const size_t smem = (size_t)d.ne * (sizeof(int) + 2 * sizeof(dfl));
   // each launch draws tiles from a fresh counter
   cudaError_t e = cudaMemsetAsync(d.counters + 3, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
+  if (pw_variant_of(d) == TC_VARIANT) {
+    if (!d.tc_B || !d.tc_max) return cudaErrorInvalidValue;
+    // spectra -> fp16 B fragments, scaled by a power of two set by their largest component
+    e = cudaMemsetAsync(d.tc_max, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    tc_absmax_kernel<<<304, 256, 0, s>>>(d, d.tc_max);
+    const int n_ap = (d.na + TC_NA - 1) / TC_NA;
+    const size_t n = (size_t)n_ap * d.K * d.tc_S * 96;
+    tc_prep_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, n_ap);
+  }
   pw_pick(d)<<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, ntz);
   return cudaGetLastError();
 }

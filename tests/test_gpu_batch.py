@@ -124,3 +124,31 @@ def test_boundary_strategies_agree(gpu, win):
                 plan.set_kernel_variant(bad)
         plan.set_kernel_variant(0)
         plan.close()
+
+
+@pytest.mark.parametrize("win", [windows.boxcar(), windows.hann(), windows.tukey(0.5), windows.triangular()],
+                         ids=["boxcar", "hann", "tukey", "triangular"])
+def test_tensor_core_variant(gpu, win):
+    """Variant 9 (mma.sync with fp16 hi/lo operands) against variant 1 and the FP64 oracle."""
+    import torch
+    rng = np.random.default_rng(31)
+    for ne, na, nt, side in [(48, 11, 1024, 40), (45, 13, 768, 36), (36, 5, 512, 24), (29, 1, 512, 20)]:
+        arr = synth.LinearArray(ne, PITCH, 0.918 * PITCH)
+        px = (np.arange(side) - (side - 1) / 2.0) * PITCH / 3
+        pz = 5e-3 + np.arange(side + 3) * PITCH / 3
+        angles = np.zeros(1) if na == 1 else np.deg2rad(np.linspace(-8.0, 8.0, na))
+        sc = synth.random_points(rng, 6, (px[0], px[-1]), (pz[0], pz[-1]))
+        rf_np = synth.pw_rf(rng, arr, sc, list(angles), nt, 20e6, 1540.0)
+        rf = torch.tensor(rf_np, dtype=torch.float32, device=gpu)
+        plan = das.PWPlan(px, pz, nt, ne, 20e6, angles, arr.width, arr.pitch, 1540.0, [2e6, 7e6], 0.0, win, FN)
+        plan.set_kernel_variant(1)
+        ref = plan.execute(rf).cpu().numpy()
+        plan.set_kernel_variant(9)
+        w = torch.empty((plan.n_x, plan.n_z), dtype=torch.float32, device=gpu)
+        img = plan.execute(rf, weights=w).cpu().numpy()
+        assert plan.info()["kernel_variant"] == 9
+        assert np.linalg.norm(img - ref) / np.linalg.norm(ref) < 1e-5, (ne, na)
+        o = sum(O.das_pw_mex(px, pz, rf_np[a].T.astype(np.float64), 20e6, angles[a], arr.width, arr.pitch, 1540.0,
+                             (2e6, 7e6), 0.0, win.spec(), FN.spec(), "on")[0] for a in range(na))
+        assert np.linalg.norm(img[0].T - o) / np.linalg.norm(o) < 1e-4, (ne, na)
+        plan.close()
