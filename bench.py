@@ -147,6 +147,8 @@ class Clocks:
 
 def pw_kernel_name(variant, window):
     """Name of the plane-wave fused kernel a plan's variant launches."""
+    if variant == 9:
+        return "pw_tc_kernel<%s> (mma.sync m16n8k16, fp16 hi/lo operands)" % window
     shapes = {1: (1, 11), 2: (2, 4), 3: (2, 2), 4: (4, 1)}
     ept, na = shapes[(variant - 1) % 4 + 1]
     return "%s<%d,%d,%s>" % ("pw_event_kernel" if variant <= 4 else "pw_fused_kernel", ept, na, window)
@@ -290,6 +292,16 @@ def run_ours(args):
             "executed_terms": info["executed_terms"],
             "peak_source": "measured FP32 FMA throughput (fnum_diag_fp32_peak); MEASURED_PEAKS.json "
             "holds only HBM and bf16 figures"}
+    if args.kernel == "fused" and info["kernel_variant"] == 9:
+        # the tensor pipe: three m16n8k16 products per 16 voxels x 8 elements x 4 angles
+        mpeak = _lib.C.c_double(0.0)
+        _lib.check(_lib.lib().fnum_diag_mma_f16_peak(local, _lib.C.byref(mpeak)))
+        na_pass = min(12, len(wl.angles))
+        mma_flops = info["executed_terms"] / (16.0 * 8.0 * na_pass) * 3 * 3 * 2 * 16 * 8 * 16  # 3 n-tiles
+        roof["tensor"] = {"achieved": mma_flops / (bf_avg_ms * 1e-3) / 1e12, "peak": mpeak.value,
+                          "unit": "TFLOP/s", "frac": mma_flops / (bf_avg_ms * 1e-3) / 1e12 / mpeak.value,
+                          "work": "mma.sync m16n8k16 instructions issued (3 fp16 products per operand tile)",
+                          "peak_source": "measured mma.sync m16n8k16 f16/f32 throughput (fnum_diag_mma_f16_peak)"}
     if rank != 0:
         return
     cb = None

@@ -18,7 +18,7 @@ EXPORTS = (
     "fnum_plan_info_get", "fnum_plan_f_numbers", "fnum_plan_destroy", "fnum_diag_fp32_peak",
     "fnum_das_pw_noalloc", "fnum_bmode", "fnum_plan_autotune", "fnum_batch_create", "fnum_batch_execute",
     "fnum_batch_frame_times", "fnum_batch_destroy", "fnum_pw_plan_set_sound_speed", "fnum_pw_sharpness_grad",
-    "fnum_plan_m_signal", "fnum_plan_set_kernel_variant",
+    "fnum_plan_m_signal", "fnum_plan_set_kernel_variant", "fnum_diag_mma_f16_peak",
 )
 
 ABI_VERSION = 3   # FNUM_ABI_VERSION of include/fnum.h
@@ -160,6 +160,8 @@ def lib():
     L.fnum_plan_destroy.argtypes = [C.c_void_p]
     L.fnum_diag_fp32_peak.restype = C.c_int
     L.fnum_diag_fp32_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    L.fnum_diag_mma_f16_peak.restype = C.c_int
+    L.fnum_diag_mma_f16_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.fnum_das_pw_noalloc.restype = C.c_int
     L.fnum_das_pw_noalloc.argtypes = [C.POINTER(PWDesc), _dp, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                       C.c_void_p]

@@ -712,6 +712,8 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
     if ((s = P->alloc(&D.tc_B, n_tc))) goto fail;
     if ((s = P->alloc(&D.tc_max, 1))) goto fail;
     P->info.scratch_bytes += (long long)(n_tc * sizeof(uint4) + sizeof(unsigned));
+    // the default variant may now be the tensor-core one
+    P->grid = std::min(fnum::pw_fused_grid(D, &bps), P->max_grid);
   }
   {
     cudaError_t e = fnum::launch_twiddles(P->tw, b.N, 0);

@@ -1001,7 +1001,8 @@ pw_event_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
 // that lanes 0..15 of each warp fill ahead of the bins.
 constexpr int TC_WARPS = NTHREADS / 32;
 constexpr int TC_EP = 16;   // elements per pass (two mma k-steps of 8 complex elements)
-constexpr int TC_TB = 32;   // bins per aperture table and per flush
+constexpr int TC_TB = 32;   // bins per flush and receive-phasor re-anchoring
+constexpr int TC_TT = 16;   // bins per aperture table
 
 __device__ __forceinline__ void tc_split(float x0, float x1, unsigned& hi, unsigned& lo) {
   const __half2 h = __floats2half2_rn(x0, x1);
@@ -1080,7 +1081,7 @@ __global__ void __launch_bounds__(256) tc_prep_kernel(const PWDev d, int n_ap) {
 template <int WIN>
 __global__ void __launch_bounds__(NTHREADS, 4)
 pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weights, int n_tiles_x, int n_tiles_z) {
-  __shared__ float4 apt[TC_WARPS][TC_TB][16];   // {lo | (hi+1) << 16, 1/L_left, 1/L_right, 1/W} per bin, voxel
+  __shared__ float4 apt[TC_WARPS][TC_TT][16];   // {lo | (hi+1) << 16, 1/L_left, 1/L_right, 1/W} per bin, voxel
   __shared__ int e_range[2];
   __shared__ int s_tile;
   __shared__ int s_nseg[TC_WARPS * 16];
@@ -1090,6 +1091,8 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
   __shared__ int4 b_next[TC_WARPS * 16];
   __shared__ int b_idx[TC_WARPS * 16];
   __shared__ float4 s_acc[2][NTHREADS];   // {acc.x, acc.y, comp.x, comp.y} per voxel V
+  __shared__ float2 s_cr[8][NTHREADS];
+  __shared__ float s_dx[8][NTHREADS];
   extern __shared__ __align__(16) unsigned char dyn[];  // lb[ne], ub[ne] (dfl), ktop[ne]
   dfl* lb_s = (dfl*)dyn;
   dfl* ub_s = lb_s + d.ne;
@@ -1183,8 +1186,7 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
         if (tid == 0)
           n_exec += (unsigned long long)(kt - d.k_lb + 1) * TC_EP * min(TC_NA, d.na - a0) * (TC_WARPS * 16);
         // the thread's (voxel, element) pairs: V, element e0 + 8s + 2q + i
-        float dxa[2][2][2];
-        float2 cr[2][2][2], p[2][2][2];
+        float2 p[2][2][2];
 #pragma unroll
         for (int V = 0; V < 2; ++V) {
           const dfl xm = d.col_m[vic[V]], xu = d.col_u[vic[V]], zu2 = d.row_u2[vjc[V]];
@@ -1194,9 +1196,9 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
             for (int i = 0; i < 2; ++i) {
               const int e = min(e0 + 8 * s + 2 * q + i, d.ne - 1);
               const dfl cm = d.el_m[e];
-              dxa[V][s][i] = fabsf((cm.x - xm.x) + (cm.y - xm.y));
+              s_dx[4 * V + 2 * s + i][tid] = fabsf((cm.x - xm.x) + (cm.y - xm.y));
               const float2 r = cis_ku(1, df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2)));
-              cr[V][s][i] = make_float2(r.x, -r.y);
+              s_cr[4 * V + 2 * s + i][tid] = make_float2(r.x, -r.y);
             }
         }
         float H[3][4];
@@ -1219,23 +1221,6 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
         const uint4* Bpe = Bp + (size_t)(e0 >> 3) * 96 + lane;
         for (int kc_hi = kt; kc_hi >= d.k_lb; kc_hi -= TC_TB) {
           const int kc_lo = max(d.k_lb, kc_hi - (TC_TB - 1));
-          __syncwarp();
-          if (lane < 16) {
-            int bs = b_idx[bv];
-            float4 bent = b_ent[bv];
-            int4 bnext = b_next[bv];
-            for (int k = kc_hi; k >= kc_lo; --k) {
-              if (k == bnext.x) {
-                bent = entry_of(bnext);
-                ++bs;
-                bnext = bseg[min(bs + 1, bnseg)];
-              }
-              apt[warp][kc_hi - k][lane] = bent;
-            }
-            b_ent[bv] = bent;
-            b_next[bv] = bnext;
-            b_idx[bv] = bs;
-          }
           // receive phasors re-anchored exactly at the chunk's first bin
 #pragma unroll
           for (int V = 0; V < 2; ++V) {
@@ -1248,54 +1233,75 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
                 p[V][s][i] = cis_ku(kc_hi, df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2)));
               }
           }
-          __syncwarp();
-          for (int k = kc_hi; k >= kc_lo; --k) {
-            float4 en[2];
-            en[0] = apt[warp][kc_hi - k][g];
-            en[1] = apt[warp][kc_hi - k][g + 8];
-            // H <- H t
-#pragma unroll
-            for (int j = 0; j < 3; ++j)
-#pragma unroll
-              for (int V = 0; V < 2; ++V) {
-                const float hr = H[j][2 * V], hi = H[j][2 * V + 1];
-                const float2 t = tph[V][j];
-                H[j][2 * V] = fmaf(hr, t.x, -hi * t.y);
-                H[j][2 * V + 1] = fmaf(hr, t.y, hi * t.x);
-              }
-            const uint4* Bk = Bpe + (size_t)(k - d.k_lb) * d.tc_S * 96;
-#pragma unroll
-            for (int s = 0; s < 2; ++s) {
-              uint4 bf[3];
-#pragma unroll
-              for (int j = 0; j < 3; ++j) bf[j] = __ldg(Bk + s * 96 + j * 32);
-              float rre[2][2], rim[2][2];
-#pragma unroll
-              for (int V = 0; V < 2; ++V) {
-                const int lohi = __float_as_int(en[V].x);
-                const int lo = lohi & 0xffff, hi = (lohi >> 16) - 1;
-#pragma unroll
-                for (int i = 0; i < 2; ++i) {
-                  const int e = e0 + 8 * s + 2 * q + i;
-                  const float invL = (e < emid[V]) ? en[V].y : en[V].z;
-                  const float w = win_t<WIN>(d.window_par, inv_par, dxa[V][s][i] * invL);
-                  const float b = (e >= lo && e <= hi) ? w * en[V].w : 0.0f;
-                  const float2 pp = p[V][s][i];
-                  rre[V][i] = b * pp.x;
-                  rim[V][i] = b * pp.y;
-                  p[V][s][i] = cmul(pp, cr[V][s][i]);
+          for (int kt_hi = kc_hi; kt_hi >= kc_lo; kt_hi -= TC_TT) {
+            const int kt_lo = max(kc_lo, kt_hi - (TC_TT - 1));
+            __syncwarp();
+            if (lane < 16) {
+              int bs = b_idx[bv];
+              float4 bent = b_ent[bv];
+              int4 bnext = b_next[bv];
+              for (int k = kt_hi; k >= kt_lo; --k) {
+                if (k == bnext.x) {
+                  bent = entry_of(bnext);
+                  ++bs;
+                  bnext = bseg[min(bs + 1, bnseg)];
                 }
+                apt[warp][kt_hi - k][lane] = bent;
               }
-              unsigned ah[4], al[4];
-              tc_split(rre[0][0], rre[0][1], ah[0], al[0]);
-              tc_split(rre[1][0], rre[1][1], ah[1], al[1]);
-              tc_split(rim[0][0], rim[0][1], ah[2], al[2]);
-              tc_split(rim[1][0], rim[1][1], ah[3], al[3]);
+              b_ent[bv] = bent;
+              b_next[bv] = bnext;
+              b_idx[bv] = bs;
+            }
+            __syncwarp();
+            for (int k = kt_hi; k >= kt_lo; --k) {
+              float4 en[2];
+              en[0] = apt[warp][kt_hi - k][g];
+              en[1] = apt[warp][kt_hi - k][g + 8];
+              // H <- H t
 #pragma unroll
-              for (int j = 0; j < 3; ++j) {
-                tc_mma(H[j], ah, bf[j].x, bf[j].y);
-                tc_mma(H[j], ah, bf[j].z, bf[j].w);
-                tc_mma(H[j], al, bf[j].x, bf[j].y);
+              for (int j = 0; j < 3; ++j)
+#pragma unroll
+                for (int V = 0; V < 2; ++V) {
+                  const float hr = H[j][2 * V], hi = H[j][2 * V + 1];
+                  const float2 t = tph[V][j];
+                  H[j][2 * V] = fmaf(hr, t.x, -hi * t.y);
+                  H[j][2 * V + 1] = fmaf(hr, t.y, hi * t.x);
+                }
+              const uint4* Bk = Bpe + (size_t)(k - d.k_lb) * d.tc_S * 96;
+#pragma unroll
+              for (int s = 0; s < 2; ++s) {
+                uint4 bf[3];
+#pragma unroll
+                for (int j = 0; j < 3; ++j) bf[j] = __ldg(Bk + s * 96 + j * 32);
+                float rre[2][2], rim[2][2];
+#pragma unroll
+                for (int V = 0; V < 2; ++V) {
+                  const int lohi = __float_as_int(en[V].x);
+                  const int lo = lohi & 0xffff, hi = (lohi >> 16) - 1;
+#pragma unroll
+                  for (int i = 0; i < 2; ++i) {
+                    const int e = e0 + 8 * s + 2 * q + i;
+                    const float invL = (e < emid[V]) ? en[V].y : en[V].z;
+                    const float w = win_t<WIN>(d.window_par, inv_par, s_dx[4 * V + 2 * s + i][tid] * invL);
+                    const float b = (e >= lo && e <= hi) ? w * en[V].w : 0.0f;
+                    const float2 pp = p[V][s][i];
+                    rre[V][i] = b * pp.x;
+                    rim[V][i] = b * pp.y;
+                    p[V][s][i] = cmul(pp, s_cr[4 * V + 2 * s + i][tid]);
+                  }
+                }
+                unsigned ah[4], al[4];
+                tc_split(rre[0][0], rre[0][1], ah[0], al[0]);
+                tc_split(rre[1][0], rre[1][1], ah[1], al[1]);
+                tc_split(rim[0][0], rim[0][1], ah[2], al[2]);
+                tc_split(rim[1][0], rim[1][1], ah[3], al[3]);
+                // product-major order: consecutive mma.sync update different accumulators
+#pragma unroll
+                for (int j = 0; j < 3; ++j) tc_mma(H[j], ah, bf[j].x, bf[j].y);
+#pragma unroll
+                for (int j = 0; j < 3; ++j) tc_mma(H[j], ah, bf[j].z, bf[j].w);
+#pragma unroll
+                for (int j = 0; j < 3; ++j) tc_mma(H[j], al, bf[j].x, bf[j].y);
               }
             }
           }
@@ -1400,17 +1406,20 @@ static pw_kernel_t pw_variant_kernel(int v, int window_id) {
     default: return pw_pick_win<4, 1>(window_id);
   }
 }
-static int pw_default_variant(int na) {
-  if (na >= 11) return 1;
-  if (na >= 4) return 2;
-  if (na >= 2) return 3;
+// default pass shape by angle count; with the fragment scratch in place the
+// tensor-core variant from 3 angles on (measured at 128 elements, 256 x 256)
+static int pw_default_variant(const PWDev& d) {
+  if (d.tc_B && d.na >= 3) return TC_VARIANT;
+  if (d.na >= 11) return 1;
+  if (d.na >= 4) return 2;
+  if (d.na >= 2) return 3;
   return 4;
 }
 static pw_kernel_t pw_pick(const PWDev& d) {
-  return pw_variant_kernel(d.variant > 0 ? d.variant : pw_default_variant(d.na), d.window_id);
+  return pw_variant_kernel(d.variant > 0 ? d.variant : pw_default_variant(d), d.window_id);
 }
 int pw_variant_count() { return 9; }
-int pw_variant_of(const PWDev& d) { return d.variant > 0 ? d.variant : pw_default_variant(d.na); }
+int pw_variant_of(const PWDev& d) { return d.variant > 0 ? d.variant : pw_default_variant(d); }
 
 static int pw_tiles_x(const PWDev& d) {
   const int tw = pw_variant_of(d) == TC_VARIANT ? TC_TILE_X : TILE_X;

@@ -490,7 +490,7 @@ class _Plan:
 
     def set_kernel_variant(self, variant):
         """Pins the fused kernel's variant (fnum_plan_set_kernel_variant): 0 = by the
-        angle count, 1..8 for a plane-wave plan."""
+        angle count, 1..9 for a plane-wave plan."""
         _lib.check(_lib.lib().fnum_plan_set_kernel_variant(self._ptr, int(variant)), self._saft)
 
 

@@ -195,7 +195,7 @@ typedef struct fnum_plan_info {
   long long scratch_bytes;         /* device scratch the plan owns */
   double scale;                    /* 2 / N_dft */
   long long executed_terms;        /* recurrence steps the fused kernel ran (>= active_terms), last execute */
-  int kernel_variant;              /* PW fused kernel variant (1..8, see fnum_plan_autotune); 0 for SA */
+  int kernel_variant;              /* PW fused kernel variant (1..9, see fnum_plan_autotune); 0 for SA */
   int grid;                        /* blocks of the fused kernel's launch */
 } fnum_plan_info;
 
@@ -244,15 +244,16 @@ int fnum_das_pw_noalloc(const fnum_pw_desc* desc, const double* steering_angles,
    fnum_plan_autotune: runs the band DFT of d_rf, then times each fused-kernel
    variant of a plane-wave plan on it (1: 1 element x 11 angles per pass,
    2: 2 x 4, 3: 2 x 2, 4: 4 x 1, with the segment boundaries resolved ahead of
-   the bin loop; 5..8: the same shapes resolving them inside the bin loop) at
-   full occupancy, and keeps the fastest
+   the bin loop; 5..8: the same shapes resolving them inside the bin loop;
+   9: tensor cores, 16 elements x 12 angles per pass, the default from 3
+   angles on) at full occupancy, and keeps the fastest
    for the plan's later executes.  It allocates a temporary image and runs on
    a private stream (not capturable).  variant / ms (the chosen variant's
    beamform time) may be NULL.  A synthetic-aperture plan has one variant:
    the call returns variant 0. */
 int fnum_plan_autotune(fnum_plan* plan, const void* d_rf, int rf_is_double, int* variant, float* ms);
 /* fnum_plan_set_kernel_variant: pins the fused-kernel variant of a plane-wave
-   plan (0 = by the angle count, 1..8 as above), e.g. one an earlier
+   plan (0 = by the angle count, 1..9 as above), e.g. one an earlier
    fnum_plan_autotune chose.  Every variant gives the same images up to the
    rounding of the per-pass sums.  A synthetic-aperture plan or a plan with
    FNUM_FLAG_M_SEMANTICS accepts only 0. */
@@ -318,6 +319,10 @@ int fnum_bmode(const void* d_image, long long n_voxels, int n_images, float floo
 /* sustained FP32 FMA throughput of the device (TFLOP/s, 2 flops per FMA): the
    roofline denominator of the fused kernels, which are bound by the FP32 pipe */
 int fnum_diag_fp32_peak(int device, double* tflops);
+/* Throughput of warp-level mma.sync m16n8k16 (fp16 operands, fp32
+   accumulators) on `device`, TFLOP/s (2 x 16 x 8 x 16 per instruction): the
+   tensor-pipe denominator of the tensor-core plane-wave kernel (variant 9). */
+int fnum_diag_mma_f16_peak(int device, double* tflops);
 
 #ifdef __cplusplus
 }

@@ -83,7 +83,7 @@ def test_autotune_keeps_results(gpu, na):
     plan, rf, (arr, px, pz, angles) = _frame(rng, 48, na, 1024, 32, True, gpu)
     ref = plan.execute(rf).cpu().numpy()
     v, ms = plan.autotune(rf)
-    assert 1 <= v <= 8 and ms > 0
+    assert 1 <= v <= 9 and ms > 0
     assert plan.info()["kernel_variant"] == v
     img = plan.execute(rf).cpu().numpy()
     assert np.linalg.norm(img - ref) / np.linalg.norm(ref) < 1e-5
@@ -119,7 +119,7 @@ def test_boundary_strategies_agree(gpu, win):
             plan.set_kernel_variant(v + 4)
             b = plan.execute(rf)
             assert torch.equal(a, b), (ne, na, v)
-        for bad in (-1, 9):
+        for bad in (-1, 10):
             with pytest.raises(_lib.FNumError):
                 plan.set_kernel_variant(bad)
         plan.set_kernel_variant(0)
