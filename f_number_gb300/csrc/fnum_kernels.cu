@@ -1091,8 +1091,8 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
   __shared__ int4 b_next[TC_WARPS * 16];
   __shared__ int b_idx[TC_WARPS * 16];
   __shared__ float4 s_acc[2][NTHREADS];   // {acc.x, acc.y, comp.x, comp.y} per voxel V
-  __shared__ float2 s_cr[8][NTHREADS];
-  __shared__ float s_dx[8][NTHREADS];
+  __shared__ float2 s_cr[8][NTHREADS];   // conj(r) of the thread's (voxel, element) pairs
+  __shared__ float2 s_dx[8][NTHREADS];   // |c_e - x| of the pairs as {left side, right side}, the other 0
   extern __shared__ __align__(16) unsigned char dyn[];  // lb[ne], ub[ne] (dfl), ktop[ne]
   dfl* lb_s = (dfl*)dyn;
   dfl* ub_s = lb_s + d.ne;
@@ -1156,14 +1156,18 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
     auto entry_of = [&](int4 c) -> float4 {
       const int ilb = code_ilb(c.y), iub = code_iub(c.y);
       const int lo = min(ilb, bemid), hi = max(iub, bemid - 1);
+      // a side whose half-width is not positive holds no element of the aperture;
+      // its 0 keeps the other side's elements (distance 0 on this side) finite
       float il = 0.0f, ir = 0.0f;
       if (ilb < d.ne) {
         const dfl l = lb_s[ilb];
-        il = __fdividef(1.0f, (bxm.x - l.x) + (bxm.y - l.y));
+        const float L = (bxm.x - l.x) + (bxm.y - l.y);
+        il = (L > 0.0f) ? __fdividef(1.0f, L) : 0.0f;
       }
       if (iub >= 0) {
         const dfl u = ub_s[iub];
-        ir = __fdividef(1.0f, (u.x - bxm.x) + (u.y - bxm.y));
+        const float L = (u.x - bxm.x) + (u.y - bxm.y);
+        ir = (L > 0.0f) ? __fdividef(1.0f, L) : 0.0f;
       }
       return make_float4(__int_as_float(lo | ((hi + 1) << 16)), il, ir, __int_as_float(c.z));
     };
@@ -1196,7 +1200,9 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
             for (int i = 0; i < 2; ++i) {
               const int e = min(e0 + 8 * s + 2 * q + i, d.ne - 1);
               const dfl cm = d.el_m[e];
-              s_dx[4 * V + 2 * s + i][tid] = fabsf((cm.x - xm.x) + (cm.y - xm.y));
+              const float dx = fabsf((cm.x - xm.x) + (cm.y - xm.y));
+              const bool left = e0 + 8 * s + 2 * q + i < emid[V];
+              s_dx[4 * V + 2 * s + i][tid] = make_float2(left ? dx : 0.0f, left ? 0.0f : dx);
               const float2 r = cis_ku(1, df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2)));
               s_cr[4 * V + 2 * s + i][tid] = make_float2(r.x, -r.y);
             }
@@ -1281,8 +1287,8 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
 #pragma unroll
                   for (int i = 0; i < 2; ++i) {
                     const int e = e0 + 8 * s + 2 * q + i;
-                    const float invL = (e < emid[V]) ? en[V].y : en[V].z;
-                    const float w = win_t<WIN>(d.window_par, inv_par, s_dx[4 * V + 2 * s + i][tid] * invL);
+                    const float2 dlr = s_dx[4 * V + 2 * s + i][tid];
+                    const float w = win_t<WIN>(d.window_par, inv_par, fmaf(dlr.x, en[V].y, dlr.y * en[V].z));
                     const float b = (e >= lo && e <= hi) ? w * en[V].w : 0.0f;
                     const float2 pp = p[V][s][i];
                     rre[V][i] = b * pp.x;
