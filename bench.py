@@ -154,8 +154,13 @@ def pw_kernel_name(variant, window):
     return "%s<%d,%d,%s>" % ("pw_event_kernel" if variant <= 4 else "pw_fused_kernel", ept, na, window)
 
 
-def traffic_from_profiles():
-    p = os.path.join(ROOT, "profiles", "pw_event_cpwc_512.json")
+def traffic_from_profiles(variant=9):
+    """DRAM bytes per launch of the launched kernel at the bench workload (ncu capture),
+    None for a variant without a capture."""
+    name = {9: "pw_tc_cpwc_512.json", 1: "pw_event_cpwc_512.json"}.get(variant)
+    if name is None:
+        return None
+    p = os.path.join(ROOT, "profiles", name)
     if os.path.exists(p):
         try:
             return json.load(open(p)).get("dram_bytes_per_launch")
@@ -285,7 +290,7 @@ def run_ours(args):
     flops = 8.0 * info["active_terms"]
     achieved = flops / (bf_avg_ms * 1e-3) / 1e12
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-            "frac": achieved / peak.value if peak.value else None, "traffic": traffic_from_profiles(),
+            "frac": achieved / peak.value if peak.value else None, "traffic": traffic_from_profiles(info["kernel_variant"]) if args.kernel == "fused" else None,
             "kernel": "pw_plain_kernel" if args.kernel == "plain" else pw_kernel_name(info["kernel_variant"], "hann"),
             "work": "8 FLOP per active voxel x element x bin x angle term "
             "(complex MAC); %d active of %d nominal terms" % (info["active_terms"], info["terms"]),
@@ -314,7 +319,7 @@ def run_ours(args):
            "gterms_per_s": info["terms"] / (ms_per_step * 1e-3) / 1e9,
            "stage_ms": {"band_dft": float(np.mean(dft_ms)), "beamform": bf_avg_ms},
            "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "clocks": clk,
-           "gpu_launches": 2 * args.steps}
+           "gpu_launches": args.steps * (4 if (args.kernel == "fused" and info["kernel_variant"] == 9) else 2)}
     print(json.dumps(out))
     plan.close()
     if dist:
@@ -421,8 +426,7 @@ def run_batch(args):
                        wl.array.width, wl.array.pitch, wl.c, list(wl.f_bounds), 0.0, windows.hann(), fn, device=0,
                        compound=True)
         rf = torch.tensor(wl.rf, dtype=torch.float32, device=dev)
-        if not args.no_autotune:
-            variants.append(p.autotune(rf)[0])
+        variants.append(p.autotune(rf)[0] if not args.no_autotune else p.info()["kernel_variant"])
         plans.append(p)
         rfs.append(rf)
         imgs.append(torch.empty((1, p.n_x, p.n_z), dtype=torch.complex64, device=dev))
@@ -467,7 +471,11 @@ def run_batch(args):
                           "in_batch_completion_p50": float(np.percentile(done, 50)),
                           "in_batch_completion_p99": float(np.percentile(done, 99)),
                           "sum_of_standalone": float(np.sum(solo))},
-           "clocks": clk, "gpu_launches": args.steps * sum(1 + (1 if p.n_out == 1 else p.n_angles) for p in plans)}
+           "clocks": clk,
+           # per frame: the band DFT, then per beamform launch the kernel (+ scale and fragment
+           # kernels for the tensor-core variant)
+           "gpu_launches": args.steps * sum(1 + (1 if p.n_out == 1 else p.n_angles) * (3 if v == 9 else 1)
+                                            for p, v in zip(plans, variants))}
     print(json.dumps(out))
     batch.close()
     for p in plans:
