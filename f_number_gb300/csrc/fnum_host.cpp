@@ -821,6 +821,13 @@ int make_sa_plan(const fnum_sa_desc* d, int flags, fnum_plan** out) {
   if ((s = P->alloc(&P->tw, b.N))) goto fail;
   if ((s = P->alloc(&P->X, (size_t)ne * ne * bk.K))) goto fail;
   D.X = P->X;
+  // transmit/receive symmetry: boxcar windows on both sides, equal F-number tables and
+  // normalisations make the weight and phase of (t, r) and (r, t) equal
+  D.Xs = nullptr;
+  if (d->window_tx.id == FNUM_WINDOW_BOXCAR && d->window_rx.id == FNUM_WINDOW_BOXCAR && Ftx == Frx &&
+      on_tx == on_rx && !(flags & FNUM_FLAG_PLAIN_KERNEL)) {
+    if ((s = P->alloc(&D.Xs, (size_t)ne * ne * bk.K))) goto fail;
+  }
   if ((s = P->alloc(&P->counters, 8))) goto fail;
   D.counters = P->counters;
   if (cudaMemset(P->counters, 0, 8 * sizeof(unsigned long long)) != cudaSuccess) {
@@ -835,6 +842,7 @@ int make_sa_plan(const fnum_sa_desc* d, int flags, fnum_plan** out) {
     if ((s = P->alloc(&seg, (size_t)P->grid * fnum::NTHREADS * D.seg_cap * fnum::SA_SEG_INT4))) goto fail;
     D.seg = seg;
     P->info.scratch_bytes = (long long)P->grid * fnum::NTHREADS * D.seg_cap * fnum::SA_SEG_INT4 * (long long)sizeof(int4);
+    if (D.Xs) P->info.scratch_bytes += (long long)ne * ne * bk.K * (long long)sizeof(float2);
   }
   {
     cudaError_t e = fnum::launch_twiddles(P->tw, b.N, 0);

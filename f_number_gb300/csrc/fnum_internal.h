@@ -99,6 +99,10 @@ struct SADev {
   const dfl* el_u; const dfl* el_m; const dfl* el_lb; const dfl* el_ub;
   const dfl* gtx; const dfl* grx;   // [K]
   float2* X;                        // [ntx][nrx][K]
+  // transmit/receive symmetry (equal windows, F-numbers and normalisations): pairs
+  // (t, r) and (r, t) share weight and phase, so Xs[t][r] = X[t][r] + X[r][t] for
+  // t < r (Xs[t][t] = X[t][t]) and only r >= t is beamformed; nullptr = off
+  float2* Xs;
   int4* seg;                        // [grid][NTHREADS][seg_cap]
   unsigned long long* counters;
   const float* px_f; const float* pz_f; const float* ctr_f; const float* lb_f; const float* ub_f;

@@ -1684,12 +1684,13 @@ __device__ __forceinline__ float sa_apod(const dfl* lb_s, const dfl* ub_s, dfl x
 // out [bin][receive] with rows of ROW float2; consecutive threads copy
 // consecutive bins of one receive element.
 template <int EPT>
-__device__ __forceinline__ void sa_stage_chunk(float2* dst, const SADev& d, int t, int r0, int kc_lo, int nk, int tid) {
+__device__ __forceinline__ void sa_stage_chunk(float2* dst, const SADev& d, int t, int r0, int kc_lo, int nk, int tid,
+                                               const float2* X) {
   constexpr int ROW = (EPT + 1) & ~1;
   for (int idx = tid; idx < KCHUNK * EPT; idx += NTHREADS) {
     const int kk = idx % KCHUNK, q = idx / KCHUNK;
     const int r = r0 + q;
-    if (kk < nk && r < d.ne) cp_async8(&dst[kk * ROW + q], &d.X[((size_t)t * d.ne + r) * d.K + (kc_lo - d.k_lb + kk)]);
+    if (kk < nk && r < d.ne) cp_async8(&dst[kk * ROW + q], &X[((size_t)t * d.ne + r) * d.K + (kc_lo - d.k_lb + kk)]);
     else if (kk < nk) dst[kk * ROW + q] = make_float2(0.0f, 0.0f);
   }
   cp_async_commit();
@@ -1716,6 +1717,7 @@ sa_fused_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
   int4* seg = d.seg + ((size_t)blockIdx.x * NTHREADS + tid) * (size_t)d.seg_cap * SA_SEG_INT4;
   const float ipt = (d.wtx_par > 0.0f) ? 1.0f / d.wtx_par : 0.0f;
   const float ipr = (d.wrx_par > 0.0f) ? 1.0f / d.wrx_par : 0.0f;
+  const float2* Xsrc = d.X;
   unsigned long long n_exec = 0;
   if (tid == 0) s_count[0] = s_count[1] = 0ull;
   for (int e = tid; e < d.ne; e += NTHREADS) {
@@ -1808,14 +1810,14 @@ sa_fused_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
         float2 part = make_float2(0.0f, 0.0f);
         const int c_top = (kt - d.k_lb) / KCHUNK;
         __syncthreads();  // every thread is done with both buffers of the previous pass
-        sa_stage_chunk<EPT>(xs[0], d, t, r0, d.k_lb + c_top * KCHUNK, kt - (d.k_lb + c_top * KCHUNK) + 1, tid);
+        sa_stage_chunk<EPT>(xs[0], d, t, r0, d.k_lb + c_top * KCHUNK, kt - (d.k_lb + c_top * KCHUNK) + 1, tid, Xsrc);
         int buf = 0;
         for (int chunk = c_top; chunk >= 0; --chunk) {
           const int kc_lo = d.k_lb + chunk * KCHUNK;
           const int kc_hi = (chunk == c_top) ? kt : kc_lo + KCHUNK - 1;
           cp_async_wait_all();
           __syncthreads();
-          if (chunk > 0) sa_stage_chunk<EPT>(xs[buf ^ 1], d, t, r0, kc_lo - KCHUNK, KCHUNK, tid);
+          if (chunk > 0) sa_stage_chunk<EPT>(xs[buf ^ 1], d, t, r0, kc_lo - KCHUNK, KCHUNK, tid, Xsrc);
           const float2* xb = xs[buf];
           buf ^= 1;
           for (int k = kc_hi; k >= kc_lo; --k) {
@@ -1933,6 +1935,7 @@ sa_event_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
   const int n_tiles = n_tiles_x * n_tiles_z;
   int4* seg = d.seg + ((size_t)blockIdx.x * NTHREADS + tid) * (size_t)d.seg_cap * SA_SEG_INT4;
   const float ipt = (d.wtx_par > 0.0f) ? 1.0f / d.wtx_par : 0.0f;
+  const float2* Xsrc = d.Xs ? d.Xs : d.X;
   unsigned long long n_exec = 0;
   if (tid == 0) s_count[0] = s_count[1] = 0ull;
   for (int e = tid; e < d.ne; e += NTHREADS) {
@@ -1981,7 +1984,7 @@ sa_event_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
       const dfl ctm = d.el_m[t];
       const float dxt = fabsf((ctm.x - xm.x) + (ctm.y - xm.y));
       const dfl utx = df_sqrt(df_add(df_sqr(df_sub(d.el_u[t], xu)), zu2));
-      for (int r0 = R_lo; r0 <= R_hi; r0 += EPT) {
+      for (int r0 = d.Xs ? max(R_lo, t) : R_lo; r0 <= R_hi; r0 += EPT) {
         int kt = -1;
 #pragma unroll
         for (int q = 0; q < EPT; ++q)
@@ -2022,14 +2025,14 @@ sa_event_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
         float2 part = make_float2(0.0f, 0.0f);
         const int c_top = (kt - d.k_lb) / KCHUNK;
         __syncthreads();  // every thread is done with both buffers of the previous pass
-        sa_stage_chunk<EPT>(xs[0], d, t, r0, d.k_lb + c_top * KCHUNK, kt - (d.k_lb + c_top * KCHUNK) + 1, tid);
+        sa_stage_chunk<EPT>(xs[0], d, t, r0, d.k_lb + c_top * KCHUNK, kt - (d.k_lb + c_top * KCHUNK) + 1, tid, Xsrc);
         int buf = 0;
         for (int chunk = c_top; chunk >= 0; --chunk) {
           const int kc_lo = d.k_lb + chunk * KCHUNK;
           const int kc_hi = (chunk == c_top) ? kt : kc_lo + KCHUNK - 1;
           cp_async_wait_all();
           __syncthreads();
-          if (chunk > 0) sa_stage_chunk<EPT>(xs[buf ^ 1], d, t, r0, kc_lo - KCHUNK, KCHUNK, tid);
+          if (chunk > 0) sa_stage_chunk<EPT>(xs[buf ^ 1], d, t, r0, kc_lo - KCHUNK, KCHUNK, tid, Xsrc);
           const float2* xb = xs[buf];
           buf ^= 1;
           for (int ks_hi = kc_hi; ks_hi >= kc_lo; ks_hi -= SA_EV_BINS) {
@@ -2165,11 +2168,33 @@ int sa_fused_grid(const SADev& d, int* blocks_per_sm) {
   return tiles < nsm * bps ? tiles : nsm * bps;
 }
 
+// Xs[t][r] = X[t][r] + X[r][t] for t < r and X[t][t] for t = r; the lower triangle is not read
+__global__ void __launch_bounds__(256) sa_symmetrize_kernel(const SADev d) {
+  const size_t n = (size_t)d.ne * d.ne * d.K;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(i % d.K);
+    const size_t tr = i / d.K;
+    const int r = (int)(tr % d.ne), t = (int)(tr / d.ne);
+    if (r < t) continue;
+    float2 x = d.X[i];
+    if (r > t) {
+      const float2 y = d.X[((size_t)r * d.ne + t) * d.K + k];
+      x.x += y.x;
+      x.y += y.y;
+    }
+    d.Xs[i] = x;
+  }
+}
+
 cudaError_t launch_sa_fused(const SADev& d, int grid, float2* image, float* wtx, float* wrx, cudaStream_t s) {
   const int ntx = (d.nx + TILE_X - 1) / TILE_X, ntz = (d.nz + TILE_Z - 1) / TILE_Z;
   // each launch draws tiles from a fresh counter
   cudaError_t e = cudaMemsetAsync(d.counters + 3, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
+  if (d.Xs) {
+    if (d.wrx_id != 0) return cudaErrorInvalidValue;  // symmetry is served by the boxcar-receive kernel
+    sa_symmetrize_kernel<<<1216, 256, 0, s>>>(d);
+  }
   sa_pick(d.wtx_id, d.wrx_id)<<<grid, NTHREADS, sa_smem(d), s>>>(d, image, wtx, wrx, ntx, ntz,
                                                                   d.last_bin_only < 0 ? 1 : 0);
   return cudaGetLastError();

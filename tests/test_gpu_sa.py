@@ -91,3 +91,27 @@ def test_sa_full_size_sampled(gpu):
                                  ix, iz)
     assert rel_l2(img[iz, ix], ref) < TOL_L2
     np.testing.assert_allclose(wt[iz, ix], rwt, rtol=TOL_W)
+
+
+@pytest.mark.parametrize("ntx,nrx", [("on", "on"), ("off", "off"), ("on", "off")])
+@pytest.mark.parametrize("ftx_kind", ["same", "other"])
+def test_sa_transmit_receive_symmetry(gpu, ntx, nrx, ftx_kind):
+    """Boxcar windows with equal F-numbers and normalisations beamform only r >= t from
+    X[t][r] + X[r][t]; the RF here is not reciprocal (independent noise per pair), so a
+    path that assumed X[t][r] = X[r][t] would fail.  Unequal settings keep all pairs."""
+    arr = synth.LinearArray(18, 0.3e-3, 0.918 * 0.3e-3)
+    rng = np.random.default_rng(41)
+    rf = rng.standard_normal((18, 18, 320))
+    px = np.linspace(-2e-3, 2e-3, 9)
+    pz = np.linspace(3e-3, 9e-3, 7)
+    data = np.transpose(rf, (2, 1, 0))
+    fn = f_numbers.directivity.perrot(0.918)
+    ftx = fn if ftx_kind == "same" else f_numbers.grating.angle_lb(60, 1.5)
+    box = windows.boxcar()
+    img, wtx, wrx = das.gpu_bf_saft_rf(px, pz, data, 40e6, arr.width, arr.pitch, 1540.0, [2e6, 9e6], 0, box, box,
+                                       ftx, fn, NORMS[ntx], NORMS[nrx], 0, semantics="intended")
+    ref, rwt, rwr, _ = O.das_sa_mex(px, pz, data, 40e6, arr.width, arr.pitch, 1540.0, (2e6, 9e6), 0.0, box.spec(),
+                                    box.spec(), ftx.spec(), fn.spec(), ntx, nrx, semantics="intended")
+    assert rel_l2(img, ref) < TOL_L2
+    np.testing.assert_allclose(wtx, rwt, rtol=TOL_W)
+    np.testing.assert_allclose(wrx, rwr, rtol=TOL_W)
