@@ -51,7 +51,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
         with ThreadPoolExecutor(max_workers=len(cmds)) as ex:
             list(ex.map(run, cmds))
         tmp_lib = os.path.join(tmp, "libfnum.so")
-        run([cc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp_lib] + objs)
+        cuda_lib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(cc))), "lib64")
+        run([cc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp_lib] + objs +
+            ["-lcublas", "-Xlinker", "-rpath", "-Xlinker", cuda_lib])
         shutil.move(tmp_lib, LIB)
     return LIB
 

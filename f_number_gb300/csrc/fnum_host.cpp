@@ -5,6 +5,7 @@
 #include "../../include/fnum.h"
 #include "fnum_internal.h"
 
+#include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <float.h>
 #include <math.h>
@@ -455,6 +456,10 @@ struct fnum_plan {
   float2* adj_gX = nullptr;
   double* adj_sums = nullptr;
   bool adj_invw_ready = false;
+  // band DFT as a GEMM: cuBLAS handle, twiddle matrix [nt][2K], PW reorder buffer
+  cublasHandle_t blas = nullptr;
+  float* dftW = nullptr;
+  float2* dftC = nullptr;
 
   template <typename T>
   int alloc(T** p, size_t count) {
@@ -477,6 +482,7 @@ struct fnum_plan {
     return FNUM_OK;
   }
   ~fnum_plan() {
+    if (blas) cublasDestroy(blas);
     for (void* p : allocs) cudaFree(p);
   }
 };
@@ -582,6 +588,31 @@ int check_sa(const fnum_sa_desc* d) {
   if (d->normalization_tx < 0 || d->normalization_tx > 2 || d->normalization_rx < 0 || d->normalization_rx > 2)
     return FNUM_ERR_NORMALIZATION;
   return check_device(d->device);
+}
+
+// Band DFT of float RF as one SGEMM (FP32 arithmetic, CUBLAS_PEDANTIC_MATH): the
+// twiddle matrix is built once from the plan's FP64 twiddle table.  Without a cuBLAS
+// handle the plan keeps the band-DFT kernel.
+int setup_gemm_dft(fnum_plan* P, int k_lb, int K, size_t pw_signals) {
+  if (cublasCreate(&P->blas) != CUBLAS_STATUS_SUCCESS) {
+    P->blas = nullptr;
+    return FNUM_OK;
+  }
+  int s;
+  void* ws = nullptr;
+  const size_t ws_bytes = 4u << 20;   // fixed workspace: no allocation inside a captured graph
+  if ((s = P->alloc((char**)&ws, ws_bytes))) return s;
+  if (cublasSetWorkspace(P->blas, ws, ws_bytes) != CUBLAS_STATUS_SUCCESS ||
+      cublasSetMathMode(P->blas, CUBLAS_PEDANTIC_MATH) != CUBLAS_STATUS_SUCCESS) {
+    cublasDestroy(P->blas);
+    P->blas = nullptr;
+    return FNUM_OK;
+  }
+  if ((s = P->alloc(&P->dftW, (size_t)P->nt * 2 * K))) return s;
+  if (pw_signals && (s = P->alloc(&P->dftC, pw_signals * K))) return s;
+  cudaError_t e = fnum::launch_dft_matrix(P->tw, P->band.N, P->nt, k_lb, K, P->dftW, 0);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  return e == cudaSuccess ? FNUM_OK : cuda_status(e);
 }
 
 int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags, fnum_plan** out) {
@@ -723,6 +754,7 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
       goto fail;
     }
   }
+  if ((s = setup_gemm_dft(P, D.k_lb, D.K, (size_t)na * ne))) goto fail;
   P->n_out = (flags & FNUM_FLAG_COMPOUND) ? 1 : na;
   P->hx.assign(d->positions_x, d->positions_x + nx);
   P->hz.assign(d->positions_z, d->positions_z + nz);
@@ -821,10 +853,10 @@ int make_sa_plan(const fnum_sa_desc* d, int flags, fnum_plan** out) {
   if ((s = P->alloc(&P->tw, b.N))) goto fail;
   if ((s = P->alloc(&P->X, (size_t)ne * ne * bk.K))) goto fail;
   D.X = P->X;
-  // transmit/receive symmetry: boxcar windows on both sides, equal F-number tables and
-  // normalisations make the weight and phase of (t, r) and (r, t) equal
+  // transmit/receive symmetry: equal windows, F-number tables and normalisations make the
+  // weight and phase of (t, r) and (r, t) equal
   D.Xs = nullptr;
-  if (d->window_tx.id == FNUM_WINDOW_BOXCAR && d->window_rx.id == FNUM_WINDOW_BOXCAR && Ftx == Frx &&
+  if (d->window_tx.id == d->window_rx.id && d->window_tx.parameter == d->window_rx.parameter && Ftx == Frx &&
       on_tx == on_rx && !(flags & FNUM_FLAG_PLAIN_KERNEL)) {
     if ((s = P->alloc(&D.Xs, (size_t)ne * ne * bk.K))) goto fail;
   }
@@ -852,6 +884,7 @@ int make_sa_plan(const fnum_sa_desc* d, int flags, fnum_plan** out) {
       goto fail;
     }
   }
+  if ((s = setup_gemm_dft(P, D.k_lb, D.K, 0))) goto fail;
   P->n_out = 1;
   P->info.N_dft = b.N; P->info.k_lb = bk.k_lb; P->info.k_ub = bk.k_ub; P->info.n_bins = bk.K;
   P->info.n_x = nx; P->info.n_z = nz; P->info.n_elements = ne; P->info.n_angles = 1; P->info.n_samples = d->n_samples;
@@ -866,6 +899,20 @@ fail:
 }
 
 int plan_dft(fnum_plan* P, const void* rf, int is_double, cudaStream_t st) {
+  if (P->blas && !is_double) {
+    const bool pw = P->kind == 0;
+    const int K = pw ? P->pw.K : P->sa.K;
+    const int nsig = pw ? P->pw.na * P->pw.ne : P->sa.ne * P->sa.ne;
+    float2* C = pw ? P->dftC : P->X;
+    const float one = 1.0f, zero = 0.0f;
+    // column-major: C^T [2K x nsig] = W^T [2K x nt] . RF^T [nt x nsig]
+    if (cublasSetStream(P->blas, st) != CUBLAS_STATUS_SUCCESS ||
+        cublasSgemm(P->blas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * K, nsig, P->nt, &one, P->dftW, 2 * K, (const float*)rf,
+                    P->nt, &zero, (float*)C, 2 * K) != CUBLAS_STATUS_SUCCESS)
+      return FNUM_ERR_CUDA;
+    if (pw) return cuda_status(fnum::launch_dft_scatter_pw(C, P->pw.na, P->pw.ne, K, P->X, st));
+    return FNUM_OK;
+  }
   if (P->kind == 0) {
     const fnum::PWDev& D = P->pw;
     return cuda_status(fnum::launch_dft_pw(rf, is_double, D.na, D.ne, P->nt, P->tw, P->band.N, D.k_lb, D.K, P->X, st));
@@ -909,6 +956,7 @@ int run_host(fnum_plan* P, const double* rf, size_t rf_count, float* re, float* 
   const size_t nvox = (size_t)P->info.n_x * P->info.n_z;
   const size_t nimg = nvox * P->n_out;
   double* d_rf = nullptr;
+  float* d_rf32 = nullptr;
   float2* d_img = nullptr;
   float* d_w = nullptr;
   float* d_w2 = nullptr;
@@ -923,7 +971,18 @@ int run_host(fnum_plan* P, const double* rf, size_t rf_count, float* re, float* 
     s = cuda_status(e);
     goto done;
   }
-  if ((s = plan_dft(P, d_rf, 1, 0))) goto done;
+  if (P->blas) {
+    // float RF for the GEMM band DFT (the first half of a second buffer's worth of the doubles)
+    e = cudaMalloc(&d_rf32, rf_count * sizeof(float));
+    if (e == cudaSuccess) e = fnum::launch_to_float(d_rf, d_rf32, rf_count, 0);
+    if (e != cudaSuccess) {
+      s = cuda_status(e);
+      goto done;
+    }
+    if ((s = plan_dft(P, d_rf32, 0, 0))) goto done;
+  } else if ((s = plan_dft(P, d_rf, 1, 0))) {
+    goto done;
+  }
   if ((s = plan_beamform(P, d_img, d_w, d_w2, 0))) goto done;
   h_img.resize(nimg);
   e = cudaMemcpy(h_img.data(), d_img, nimg * sizeof(float2), cudaMemcpyDeviceToHost);
@@ -951,6 +1010,7 @@ int run_host(fnum_plan* P, const double* rf, size_t rf_count, float* re, float* 
   }
 done:
   if (d_rf) cudaFree(d_rf);
+  if (d_rf32) cudaFree(d_rf32);
   if (d_img) cudaFree(d_img);
   if (d_w) cudaFree(d_w);
   if (d_w2) cudaFree(d_w2);

@@ -294,6 +294,47 @@ cudaError_t launch_dft_sa(const void* rf, int is_double, int nsig, int nt, const
   return dft_launch(rf, is_double, nsig, nt, tw, N, k_lb, K, X, 1, 0, K, nsig, s);
 }
 
+// The band DFT as a GEMM (cuBLAS SGEMM on the host side): spectra [signal][2K] =
+// RF [signal][nt] . W [nt][2K], W[t][2k'] + j W[t][2k'+1] = e^{-j 2 pi (k_lb + k') t / N}
+// with the index (k t) mod N exact in integers and the twiddles of the FP64 table.
+__global__ void dft_matrix_kernel(const float2* __restrict__ tw, int N, int nt, int k_lb, int K, float* __restrict__ W) {
+  const size_t n = (size_t)nt * K;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const long long t = (long long)(i / K), kk = (long long)(i % K);
+    const float2 w = tw[(t * (k_lb + kk)) % N];
+    W[t * 2 * K + 2 * kk] = w.x;
+    W[t * 2 * K + 2 * kk + 1] = w.y;
+  }
+}
+cudaError_t launch_dft_matrix(const float2* tw, int N, int nt, int k_lb, int K, float* W, cudaStream_t s) {
+  dft_matrix_kernel<<<1216, 256, 0, s>>>(tw, N, nt, k_lb, K, W);
+  return cudaGetLastError();
+}
+
+// PW spectra from the GEMM's [a * ne + e][k] order to the beamformer's [e][k][a]
+__global__ void dft_scatter_pw_kernel(const float2* __restrict__ C, int na, int ne, int K, float2* __restrict__ X) {
+  const size_t n = (size_t)na * ne * K;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int a = (int)(i % na);
+    const size_t ek = i / na;
+    const int k = (int)(ek % K), e = (int)(ek / K);
+    X[i] = C[((size_t)a * ne + e) * K + k];
+  }
+}
+cudaError_t launch_dft_scatter_pw(const float2* C, int na, int ne, int K, float2* X, cudaStream_t s) {
+  dft_scatter_pw_kernel<<<1216, 256, 0, s>>>(C, na, ne, K, X);
+  return cudaGetLastError();
+}
+
+__global__ void to_float_kernel(const double* __restrict__ in, float* __restrict__ out, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+cudaError_t launch_to_float(const double* in, float* out, size_t n, cudaStream_t s) {
+  to_float_kernel<<<1216, 256, 0, s>>>(in, out, n);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // fused plane-wave kernel
 // ---------------------------------------------------------------------------
@@ -1717,7 +1758,7 @@ sa_fused_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
   int4* seg = d.seg + ((size_t)blockIdx.x * NTHREADS + tid) * (size_t)d.seg_cap * SA_SEG_INT4;
   const float ipt = (d.wtx_par > 0.0f) ? 1.0f / d.wtx_par : 0.0f;
   const float ipr = (d.wrx_par > 0.0f) ? 1.0f / d.wrx_par : 0.0f;
-  const float2* Xsrc = d.X;
+  const float2* Xsrc = d.Xs ? d.Xs : d.X;
   unsigned long long n_exec = 0;
   if (tid == 0) s_count[0] = s_count[1] = 0ull;
   for (int e = tid; e < d.ne; e += NTHREADS) {
@@ -1766,7 +1807,7 @@ sa_fused_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
       const dfl ctm = d.el_m[t];
       const float dxt = fabsf((ctm.x - xm.x) + (ctm.y - xm.y));
       const dfl utx = df_sqrt(df_add(df_sqr(df_sub(d.el_u[t], xu)), zu2));
-      for (int r0 = R_lo; r0 <= R_hi; r0 += EPT) {
+      for (int r0 = d.Xs ? max(R_lo, t) : R_lo; r0 <= R_hi; r0 += EPT) {
         int kt = -1;
 #pragma unroll
         for (int q = 0; q < EPT; ++q)
@@ -2191,10 +2232,7 @@ cudaError_t launch_sa_fused(const SADev& d, int grid, float2* image, float* wtx,
   // each launch draws tiles from a fresh counter
   cudaError_t e = cudaMemsetAsync(d.counters + 3, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
-  if (d.Xs) {
-    if (d.wrx_id != 0) return cudaErrorInvalidValue;  // symmetry is served by the boxcar-receive kernel
-    sa_symmetrize_kernel<<<1216, 256, 0, s>>>(d);
-  }
+  if (d.Xs) sa_symmetrize_kernel<<<1216, 256, 0, s>>>(d);
   sa_pick(d.wtx_id, d.wrx_id)<<<grid, NTHREADS, sa_smem(d), s>>>(d, image, wtx, wrx, ntx, ntz,
                                                                   d.last_bin_only < 0 ? 1 : 0);
   return cudaGetLastError();
