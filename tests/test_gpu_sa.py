@@ -115,3 +115,19 @@ def test_sa_transmit_receive_symmetry(gpu, ntx, nrx, ftx_kind):
     assert rel_l2(img, ref) < TOL_L2
     np.testing.assert_allclose(wtx, rwt, rtol=TOL_W)
     np.testing.assert_allclose(wrx, rwr, rtol=TOL_W)
+
+
+@pytest.mark.parametrize("win", [windows.hann(), windows.tukey(0.3), windows.triangular()], ids=["hann", "tukey", "tri"])
+def test_sa_symmetry_windowed(gpu, win):
+    """Equal non-boxcar windows on both sides: the in-loop kernel with r >= t only."""
+    arr = synth.LinearArray(14, 0.3e-3, 0.918 * 0.3e-3)
+    rng = np.random.default_rng(43)
+    rf = rng.standard_normal((14, 14, 300))
+    px = np.linspace(-1.5e-3, 1.5e-3, 8)
+    pz = np.linspace(3e-3, 8e-3, 6)
+    data = np.transpose(rf, (2, 1, 0))
+    fn = f_numbers.directivity.perrot(0.918)
+    img, _, _ = das.gpu_bf_saft_rf(px, pz, data, 40e6, arr.width, arr.pitch, 1540.0, [2e6, 9e6], 0, win, win, fn, fn)
+    ref, _, _, _ = O.das_sa_mex(px, pz, data, 40e6, arr.width, arr.pitch, 1540.0, (2e6, 9e6), 0.0, win.spec(),
+                                win.spec(), fn.spec(), fn.spec(), "on", "on")
+    assert rel_l2(img, ref) < TOL_L2
