@@ -455,6 +455,7 @@ struct fnum_plan {
   float2* adj_H = nullptr;
   float2* adj_gX = nullptr;
   double* adj_sums = nullptr;
+  double* adj_acc = nullptr;   // FP64 sums of the voxel slices, 4 per spectrum entry
   bool adj_invw_ready = false;
   // band DFT as a GEMM: cuBLAS handle, twiddle matrix [nt][2K], PW reorder buffer
   cublasHandle_t blas = nullptr;
@@ -1463,7 +1464,7 @@ int fnum_pw_sharpness_grad(fnum_plan* plan, const void* d_rf, int rf_is_double, 
   if (!plan->adj_img) {
     if ((s = plan->alloc(&plan->adj_img, (size_t)nvox)) || (s = plan->alloc(&plan->adj_invw, (size_t)nvox * D.K)) ||
         (s = plan->alloc(&plan->adj_H, nspec)) || (s = plan->alloc(&plan->adj_gX, nspec)) ||
-        (s = plan->alloc(&plan->adj_sums, 4)))
+        (s = plan->alloc(&plan->adj_sums, 4)) || (s = plan->alloc(&plan->adj_acc, 4 * nspec)))
       return s;
   }
   if (!plan->adj_invw_ready) {
@@ -1486,7 +1487,7 @@ int fnum_pw_sharpness_grad(fnum_plan* plan, const void* d_rf, int rf_is_double, 
   }
   const double gs2 = 1.0 / (S[0] * S[0]), gs4 = S[1] / (S[0] * S[0] * S[0]);
   FNUM_CUDA(fnum::launch_pw_adjoint(D, plan->adj_img, plan->adj_invw, (float)gs2, (float)gs4,
-                                    (float)(plan->t0 / plan->band.N), gX, plan->adj_H, st));
+                                    (float)(plan->t0 / plan->band.N), gX, plan->adj_H, plan->adj_acc, st));
   const double coef = 4.0 * M_PI * (2.0 / plan->band.N) / plan->c;
   FNUM_CUDA(fnum::launch_pw_dldc(D, plan->adj_H, coef, plan->adj_sums + 2, st));
   double g = 0.0;

@@ -139,7 +139,7 @@ cudaError_t launch_sa_plain(const SADev& d, float2* image, float* wtx, float* wr
 cudaError_t launch_pw_invw(const PWDev& d, float* invw, cudaStream_t s);
 cudaError_t launch_pw_sharp_sums(const float2* img, long long n, double* sums, cudaStream_t s);
 cudaError_t launch_pw_adjoint(const PWDev& d, const float2* img, const float* invw, float gs2, float gs4, float t0N,
-                              float2* gX, float2* H, cudaStream_t s);
+                              float2* gX, float2* H, double* acc, cudaStream_t s);   // acc: 4 doubles per spectrum entry
 cudaError_t launch_pw_dldc(const PWDev& d, const float2* H, double coef, double* out, cudaStream_t s);
 
 }  // namespace fnum

@@ -2369,19 +2369,22 @@ __global__ void __launch_bounds__(256) pw_sharp_sums_kernel(const float2* __rest
   }
 }
 
-// One block per band bin k, one thread per element (elements beyond the block
-// size run as further passes), ADJ_NA angles per pass.  Voxels are taken in
-// batches of ADJ_VB: the block first stages, per voxel, what every element
-// shares -- the transmit phasors e^{j 2 pi k u_tx} of the pass's angles, the
-// aperture at bin k, 1/W and G -- then each thread adds its element's terms:
-// one exact receive phasor e^{j 2 pi k u_rx} per (voxel, element) times the
-// staged transmit phasors.  Each batch is summed in FP32 and added in FP64.
+// One block per (band bin k, slice of ADJ_SLICE voxels), one thread per element
+// (elements beyond the block size run as further passes), ADJ_NA angles per
+// pass.  Voxels are taken in batches of ADJ_VB: the block first stages, per
+// voxel, what every element shares -- the transmit phasors e^{j 2 pi k u_tx} of
+// the pass's angles, the aperture at bin k, 1/W and G -- then each thread adds
+// its element's terms: one exact receive phasor e^{j 2 pi k u_rx} per (voxel,
+// element) times the staged transmit phasors.  A slice is summed in FP32 and
+// the slices are added in FP64 (atomics into acc, finished by
+// pw_adjoint_finish_kernel).
 constexpr int ADJ_NA = 11;
 constexpr int ADJ_VB = 128;
+constexpr int ADJ_SLICE = 8192;   // voxels per block: the grid is bins x voxel slices
 template <int WIN>
-__global__ void __launch_bounds__(128, 2)
+__global__ void __launch_bounds__(128, 4)
 pw_adjoint_kernel(const PWDev d, const float2* __restrict__ img, const float* __restrict__ invw, float gs2, float gs4,
-                  float t0N, float2* __restrict__ gX, float2* __restrict__ H) {
+                  float t0N, double* __restrict__ acc) {
   __shared__ float2 sT[ADJ_VB][ADJ_NA];   // transmit phasor
   __shared__ float sUt[ADJ_VB][ADJ_NA];   // u_tx - t0/N
   __shared__ float2 sG[ADJ_VB];           // G_v / W_{v,k} (0: no contribution)
@@ -2390,7 +2393,9 @@ pw_adjoint_kernel(const PWDev d, const float2* __restrict__ img, const float* __
   const int tid = threadIdx.x;
   const int kk = blockIdx.x, k = d.k_lb + kk;
   const dfl g = d.g[kk];
-  const long long nvox = (long long)d.nx * d.nz;
+  const long long nvox_all = (long long)d.nx * d.nz;
+  const long long v_begin = (long long)blockIdx.y * ADJ_SLICE;
+  const long long nvox = min(nvox_all, v_begin + ADJ_SLICE);   // this slice: v_begin .. nvox - 1
   const float inv_par = (d.window_par > 0.0f) ? 1.0f / d.window_par : 0.0f;
   for (int e0 = 0; e0 < d.ne; e0 += 128) {
     const int e = e0 + tid;
@@ -2399,10 +2404,11 @@ pw_adjoint_kernel(const PWDev d, const float2* __restrict__ img, const float* __
     const dfl cm = d.el_m[ec], cu = d.el_u[ec];
     for (int a0 = 0; a0 < d.na; a0 += ADJ_NA) {
       const int nag = min(ADJ_NA, d.na - a0);
-      double sXr[ADJ_NA], sXi[ADJ_NA], sHr[ADJ_NA], sHi[ADJ_NA];
+      // the slice's sums in FP32 (at most ADJ_SLICE voxels), added across slices in FP64
+      float pXr[ADJ_NA], pXi[ADJ_NA], pHr[ADJ_NA], pHi[ADJ_NA];
 #pragma unroll
-      for (int q = 0; q < ADJ_NA; ++q) sXr[q] = sXi[q] = sHr[q] = sHi[q] = 0.0;
-      for (long long v0 = 0; v0 < nvox; v0 += ADJ_VB) {
+      for (int q = 0; q < ADJ_NA; ++q) pXr[q] = pXi[q] = pHr[q] = pHi[q] = 0.0f;
+      for (long long v0 = v_begin; v0 < nvox; v0 += ADJ_VB) {
         const int nvb = (int)min((long long)ADJ_VB, nvox - v0);
         __syncthreads();  // the previous batch is consumed
         for (int q = tid; q < nvb; q += 128) {
@@ -2430,9 +2436,6 @@ pw_adjoint_kernel(const PWDev d, const float2* __restrict__ img, const float* __
         }
         __syncthreads();
         if (!has_e) continue;
-        float pXr[ADJ_NA], pXi[ADJ_NA], pHr[ADJ_NA], pHi[ADJ_NA];
-#pragma unroll
-        for (int q = 0; q < ADJ_NA; ++q) pXr[q] = pXi[q] = pHr[q] = pHi[q] = 0.0f;
         for (int vb = 0; vb < nvb; ++vb) {
           const float2 G = sG[vb];
           if (G.x == 0.0f && G.y == 0.0f) continue;
@@ -2470,21 +2473,16 @@ pw_adjoint_kernel(const PWDev d, const float2* __restrict__ img, const float* __
             }
           }
         }
-#pragma unroll
-        for (int a = 0; a < ADJ_NA; ++a) {
-          sXr[a] += pXr[a];
-          sXi[a] += pXi[a];
-          sHr[a] += pHr[a];
-          sHi[a] += pHi[a];
-        }
       }
       if (has_e) {
 #pragma unroll
         for (int a = 0; a < ADJ_NA; ++a) {
           if (a < nag) {
-            const size_t o = ((size_t)e * d.K + kk) * d.na + a0 + a;
-            gX[o] = make_float2((float)(d.scale * sXr[a]), (float)(d.scale * sXi[a]));
-            H[o] = make_float2((float)sHr[a], (float)sHi[a]);
+            double* o = acc + 4 * (((size_t)e * d.K + kk) * d.na + a0 + a);
+            atomicAdd(o, (double)pXr[a]);
+            atomicAdd(o + 1, (double)pXi[a]);
+            atomicAdd(o + 2, (double)pHr[a]);
+            atomicAdd(o + 3, (double)pHi[a]);
           }
         }
       }
@@ -2532,15 +2530,32 @@ cudaError_t launch_pw_sharp_sums(const float2* img, long long n, double* sums, c
   return cudaGetLastError();
 }
 
-cudaError_t launch_pw_adjoint(const PWDev& d, const float2* img, const float* invw, float gs2, float gs4, float t0N,
-                              float2* gX, float2* H, cudaStream_t s) {
-  const int grid = d.K;
-  switch (d.window_id) {
-    case 0: pw_adjoint_kernel<0><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, gX, H); break;
-    case 1: pw_adjoint_kernel<1><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, gX, H); break;
-    case 2: pw_adjoint_kernel<2><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, gX, H); break;
-    default: pw_adjoint_kernel<4><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, gX, H); break;
+// FP64 sums {Xr, Xi, Hr, Hi} per (element, bin, angle) -> dL/dX* (scaled by 2/N) and H
+__global__ void __launch_bounds__(256) pw_adjoint_finish_kernel(const double* __restrict__ acc, size_t n, double scale,
+                                                                float2* __restrict__ gX, float2* __restrict__ H) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double* a = acc + 4 * i;
+    gX[i] = make_float2((float)(scale * a[0]), (float)(scale * a[1]));
+    H[i] = make_float2((float)a[2], (float)a[3]);
   }
+}
+
+cudaError_t launch_pw_adjoint(const PWDev& d, const float2* img, const float* invw, float gs2, float gs4, float t0N,
+                              float2* gX, float2* H, double* acc, cudaStream_t s) {
+  const size_t n = (size_t)d.ne * d.K * d.na;
+  cudaError_t e = cudaMemsetAsync(acc, 0, 4 * n * sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  const long long nvox = (long long)d.nx * d.nz;
+  const dim3 grid(d.K, (unsigned)((nvox + ADJ_SLICE - 1) / ADJ_SLICE));
+  switch (d.window_id) {
+    case 0: pw_adjoint_kernel<0><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, acc); break;
+    case 1: pw_adjoint_kernel<1><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, acc); break;
+    case 2: pw_adjoint_kernel<2><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, acc); break;
+    default: pw_adjoint_kernel<4><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, acc); break;
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  pw_adjoint_finish_kernel<<<608, 256, 0, s>>>(acc, n, (double)d.scale, gX, H);
   return cudaGetLastError();
 }
 
