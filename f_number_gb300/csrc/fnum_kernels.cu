@@ -1042,7 +1042,7 @@ pw_event_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
 // that lanes 0..15 of each warp fill ahead of the bins.
 constexpr int TC_WARPS = NTHREADS / 32;
 constexpr int TC_EP = 16;   // elements per pass (two mma k-steps of 8 complex elements)
-constexpr int TC_TB = 32;   // bins per flush and receive-phasor re-anchoring
+constexpr int TC_TB = 64;   // bins per flush and receive-phasor re-anchoring
 constexpr int TC_TT = 16;   // bins per aperture table
 
 __device__ __forceinline__ void tc_split(float x0, float x1, unsigned& hi, unsigned& lo) {
