@@ -739,7 +739,7 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
     P->info.scratch_bytes =
         (long long)P->max_grid * fnum::NTHREADS * D.seg_cap * fnum::PW_SEG_INT4 * (long long)sizeof(int4);
     // tensor-core variant: spectra as mma fragments (96 uint4 per bin and group of 8 elements)
-    D.tc_S = (ne + 7) / 8 + 1;
+    D.tc_S = (ne + 7) / 8 + fnum::TC_KS - 1;   // a pass may start in the last group of 8
     const size_t n_tc = (size_t)((na + fnum::TC_NA - 1) / fnum::TC_NA) * D.K * D.tc_S * 96;
     if ((s = P->alloc(&D.tc_B, n_tc))) goto fail;
     if ((s = P->alloc(&D.tc_max, 1))) goto fail;

@@ -19,6 +19,8 @@ constexpr int KCHUNK = 64;
 // tensor-core plane-wave kernel: 4 warps of 16 voxels, TC_TILE_X columns x TILE_Z rows
 constexpr int TC_TILE_X = 2;
 constexpr int TC_NA = 12;   // angles per angle pass (3 mma n-tiles of 4 complex angles)
+constexpr int TC_EP = 16;   // elements per pass: TC_KS mma k-steps of 8 complex elements
+constexpr int TC_KS = TC_EP / 8;
 constexpr int TC_VARIANT = 9;
 
 // one aperture segment of one voxel (bins k_start down to the next entry's
@@ -65,7 +67,7 @@ struct PWDev {
   // and the largest |component| of the spectra (float bits) that sets their fp16 scale
   uint4* tc_B;
   unsigned* tc_max;
-  int tc_S;            // element groups of 8 in tc_B (one zero group of padding included)
+  int tc_S;            // element groups of 8 in tc_B (TC_KS - 1 zero groups of padding included)
   unsigned long long* counters;   // [0] active terms, [1] zero-weight bins, [2] error bits,
                                   // [3] tile counter, [4] executed recurrence steps
   // the per-voxel FP32 kernel reads the reference's float geometry

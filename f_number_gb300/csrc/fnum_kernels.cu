@@ -1041,7 +1041,6 @@ pw_event_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
 // aperture data come from the segment lists through a table in shared memory
 // that lanes 0..15 of each warp fill ahead of the bins.
 constexpr int TC_WARPS = NTHREADS / 32;
-constexpr int TC_EP = 16;   // elements per pass (two mma k-steps of 8 complex elements)
 constexpr int TC_TB = 64;   // bins per flush and receive-phasor re-anchoring
 constexpr int TC_TT = 16;   // bins per aperture table
 
@@ -1132,8 +1131,8 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
   __shared__ int4 b_next[TC_WARPS * 16];
   __shared__ int b_idx[TC_WARPS * 16];
   __shared__ float4 s_acc[2][NTHREADS];   // {acc.x, acc.y, comp.x, comp.y} per voxel V
-  __shared__ float2 s_cr[8][NTHREADS];   // conj(r) of the thread's (voxel, element) pairs
-  __shared__ float2 s_dx[8][NTHREADS];   // |c_e - x| of the pairs as {left side, right side}, the other 0
+  __shared__ float2 s_cr[4 * TC_KS][NTHREADS];   // conj(r) of the thread's (voxel, element) pairs
+  __shared__ float2 s_dx[4 * TC_KS][NTHREADS];   // |c_e - x| of the pairs as {left side, right side}, the other 0
   extern __shared__ __align__(16) unsigned char dyn[];  // lb[ne], ub[ne] (dfl), ktop[ne]
   dfl* lb_s = (dfl*)dyn;
   dfl* ub_s = lb_s + d.ne;
@@ -1231,21 +1230,21 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
         if (tid == 0)
           n_exec += (unsigned long long)(kt - d.k_lb + 1) * TC_EP * min(TC_NA, d.na - a0) * (TC_WARPS * 16);
         // the thread's (voxel, element) pairs: V, element e0 + 8s + 2q + i
-        float2 p[2][2][2];
+        float2 p[2][TC_KS][2];
 #pragma unroll
         for (int V = 0; V < 2; ++V) {
           const dfl xm = d.col_m[vic[V]], xu = d.col_u[vic[V]], zu2 = d.row_u2[vjc[V]];
 #pragma unroll
-          for (int s = 0; s < 2; ++s)
+          for (int s = 0; s < TC_KS; ++s)
 #pragma unroll
             for (int i = 0; i < 2; ++i) {
               const int e = min(e0 + 8 * s + 2 * q + i, d.ne - 1);
               const dfl cm = d.el_m[e];
               const float dx = fabsf((cm.x - xm.x) + (cm.y - xm.y));
               const bool left = e0 + 8 * s + 2 * q + i < emid[V];
-              s_dx[4 * V + 2 * s + i][tid] = make_float2(left ? dx : 0.0f, left ? 0.0f : dx);
+              s_dx[2 * TC_KS * V + 2 * s + i][tid] = make_float2(left ? dx : 0.0f, left ? 0.0f : dx);
               const float2 r = cis_ku(1, df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2)));
-              s_cr[4 * V + 2 * s + i][tid] = make_float2(r.x, -r.y);
+              s_cr[2 * TC_KS * V + 2 * s + i][tid] = make_float2(r.x, -r.y);
             }
         }
         float H[3][4];
@@ -1273,7 +1272,7 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
           for (int V = 0; V < 2; ++V) {
             const dfl xu = d.col_u[vic[V]], zu2 = d.row_u2[vjc[V]];
 #pragma unroll
-            for (int s = 0; s < 2; ++s)
+            for (int s = 0; s < TC_KS; ++s)
 #pragma unroll
               for (int i = 0; i < 2; ++i) {
                 const int e = min(e0 + 8 * s + 2 * q + i, d.ne - 1);
@@ -1316,7 +1315,7 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
                 }
               const uint4* Bk = Bpe + (size_t)(k - d.k_lb) * d.tc_S * 96;
 #pragma unroll
-              for (int s = 0; s < 2; ++s) {
+              for (int s = 0; s < TC_KS; ++s) {
                 uint4 bf[3];
 #pragma unroll
                 for (int j = 0; j < 3; ++j) bf[j] = __ldg(Bk + s * 96 + j * 32);
@@ -1328,13 +1327,13 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
 #pragma unroll
                   for (int i = 0; i < 2; ++i) {
                     const int e = e0 + 8 * s + 2 * q + i;
-                    const float2 dlr = s_dx[4 * V + 2 * s + i][tid];
+                    const float2 dlr = s_dx[2 * TC_KS * V + 2 * s + i][tid];
                     const float w = win_t<WIN>(d.window_par, inv_par, fmaf(dlr.x, en[V].y, dlr.y * en[V].z));
                     const float b = (e >= lo && e <= hi) ? w * en[V].w : 0.0f;
                     const float2 pp = p[V][s][i];
                     rre[V][i] = b * pp.x;
                     rim[V][i] = b * pp.y;
-                    p[V][s][i] = cmul(pp, s_cr[4 * V + 2 * s + i][tid]);
+                    p[V][s][i] = cmul(pp, s_cr[2 * TC_KS * V + 2 * s + i][tid]);
                   }
                 }
                 unsigned ah[4], al[4];
