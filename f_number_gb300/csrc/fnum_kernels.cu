@@ -1131,7 +1131,9 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
   __shared__ int4 b_next[TC_WARPS * 16];
   __shared__ int b_idx[TC_WARPS * 16];
   __shared__ float4 s_acc[2][NTHREADS];   // {acc.x, acc.y, comp.x, comp.y} per voxel V
-  __shared__ float2 s_cr[4 * TC_KS][NTHREADS];   // conj(r) of the thread's (voxel, element) pairs
+  // conj(r) of the thread's (voxel, element) pairs, packed over the two elements i of a
+  // (voxel, k-step): {re, re}, {im, im}, {-im, -im}
+  __shared__ float2 s_cr[2 * TC_KS][3][NTHREADS];
   __shared__ float2 s_dx[4 * TC_KS][NTHREADS];   // |c_e - x| of the pairs as {left side, right side}, the other 0
   extern __shared__ __align__(16) unsigned char dyn[];  // lb[ne], ub[ne] (dfl), ktop[ne]
   dfl* lb_s = (dfl*)dyn;
@@ -1230,7 +1232,8 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
         if (tid == 0)
           n_exec += (unsigned long long)(kt - d.k_lb + 1) * TC_EP * min(TC_NA, d.na - a0) * (TC_WARPS * 16);
         // the thread's (voxel, element) pairs: V, element e0 + 8s + 2q + i
-        float2 p[2][TC_KS][2];
+        // receive phasors r^k packed over the two elements of a (voxel, k-step): {re, re}, {im, im}
+        float2 pr[2][TC_KS], pim[2][TC_KS];
 #pragma unroll
         for (int V = 0; V < 2; ++V) {
           const dfl xm = d.col_m[vic[V]], xu = d.col_u[vic[V]], zu2 = d.row_u2[vjc[V]];
@@ -1244,7 +1247,10 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
               const bool left = e0 + 8 * s + 2 * q + i < emid[V];
               s_dx[2 * TC_KS * V + 2 * s + i][tid] = make_float2(left ? dx : 0.0f, left ? 0.0f : dx);
               const float2 r = cis_ku(1, df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2)));
-              s_cr[2 * TC_KS * V + 2 * s + i][tid] = make_float2(r.x, -r.y);
+              float* c = reinterpret_cast<float*>(&s_cr[TC_KS * V + s][0][tid]);
+              c[i] = r.x;
+              reinterpret_cast<float*>(&s_cr[TC_KS * V + s][1][tid])[i] = -r.y;
+              reinterpret_cast<float*>(&s_cr[TC_KS * V + s][2][tid])[i] = r.y;
             }
         }
         float H[3][4];
@@ -1276,7 +1282,14 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
 #pragma unroll
               for (int i = 0; i < 2; ++i) {
                 const int e = min(e0 + 8 * s + 2 * q + i, d.ne - 1);
-                p[V][s][i] = cis_ku(kc_hi, df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2)));
+                const float2 c = cis_ku(kc_hi, df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2)));
+                if (i == 0) {
+                  pr[V][s].x = c.x;
+                  pim[V][s].x = c.y;
+                } else {
+                  pr[V][s].y = c.x;
+                  pim[V][s].y = c.y;
+                }
               }
           }
           for (int kt_hi = kc_hi; kt_hi >= kc_lo; kt_hi -= TC_TT) {
@@ -1319,28 +1332,34 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
                 uint4 bf[3];
 #pragma unroll
                 for (int j = 0; j < 3; ++j) bf[j] = __ldg(Bk + s * 96 + j * 32);
-                float rre[2][2], rim[2][2];
+                float2 rre[2], rim[2];
 #pragma unroll
                 for (int V = 0; V < 2; ++V) {
                   const int lohi = __float_as_int(en[V].x);
                   const int lo = lohi & 0xffff, hi = (lohi >> 16) - 1;
+                  float b[2];
 #pragma unroll
                   for (int i = 0; i < 2; ++i) {
                     const int e = e0 + 8 * s + 2 * q + i;
                     const float2 dlr = s_dx[2 * TC_KS * V + 2 * s + i][tid];
                     const float w = win_t<WIN>(d.window_par, inv_par, fmaf(dlr.x, en[V].y, dlr.y * en[V].z));
-                    const float b = (e >= lo && e <= hi) ? w * en[V].w : 0.0f;
-                    const float2 pp = p[V][s][i];
-                    rre[V][i] = b * pp.x;
-                    rim[V][i] = b * pp.y;
-                    p[V][s][i] = cmul(pp, s_cr[2 * TC_KS * V + 2 * s + i][tid]);
+                    b[i] = (e >= lo && e <= hi) ? w * en[V].w : 0.0f;
                   }
+                  // R = b r^k and r^k <- r^k conj(r), two elements per packed FP32 instruction
+                  const float2 bb = make_float2(b[0], b[1]);
+                  const float2 Pr = pr[V][s], Pi = pim[V][s];
+                  rre[V] = __fmul2_rn(bb, Pr);
+                  rim[V] = __fmul2_rn(bb, Pi);
+                  const float2 cre = s_cr[TC_KS * V + s][0][tid], cim = s_cr[TC_KS * V + s][1][tid],
+                               cimn = s_cr[TC_KS * V + s][2][tid];
+                  pr[V][s] = __ffma2_rn(Pi, cimn, __fmul2_rn(Pr, cre));
+                  pim[V][s] = __ffma2_rn(Pi, cre, __fmul2_rn(Pr, cim));
                 }
                 unsigned ah[4], al[4];
-                tc_split(rre[0][0], rre[0][1], ah[0], al[0]);
-                tc_split(rre[1][0], rre[1][1], ah[1], al[1]);
-                tc_split(rim[0][0], rim[0][1], ah[2], al[2]);
-                tc_split(rim[1][0], rim[1][1], ah[3], al[3]);
+                tc_split(rre[0].x, rre[0].y, ah[0], al[0]);
+                tc_split(rre[1].x, rre[1].y, ah[1], al[1]);
+                tc_split(rim[0].x, rim[0].y, ah[2], al[2]);
+                tc_split(rim[1].x, rim[1].y, ah[3], al[3]);
                 // product-major order: consecutive mma.sync update different accumulators
 #pragma unroll
                 for (int j = 0; j < 3; ++j) tc_mma(H[j], ah, bf[j].x, bf[j].y);
