@@ -461,6 +461,15 @@ struct fnum_plan {
   cublasHandle_t blas = nullptr;
   float* dftW = nullptr;
   float2* dftC = nullptr;
+  // device buffers of the host-buffer entry points (fnum_das_pw / fnum_das_sa), kept for the
+  // plan's life so that a cached plan runs without allocating
+  double* h_rf = nullptr;
+  float* h_rf32 = nullptr;
+  float2* h_img = nullptr;
+  float* h_planes = nullptr;   // real plane, then imaginary plane
+  float* h_w = nullptr;
+  float* h_w2 = nullptr;
+  size_t h_rf_count = 0;
 
   template <typename T>
   int alloc(T** p, size_t count) {
@@ -956,67 +965,38 @@ int plan_beamform(fnum_plan* P, void* image, float* w, float* w2, cudaStream_t s
 int run_host(fnum_plan* P, const double* rf, size_t rf_count, float* re, float* im, float* w, float* w2) {
   const size_t nvox = (size_t)P->info.n_x * P->info.n_z;
   const size_t nimg = nvox * P->n_out;
-  double* d_rf = nullptr;
-  float* d_rf32 = nullptr;
-  float2* d_img = nullptr;
-  float* d_w = nullptr;
-  float* d_w2 = nullptr;
   int s = FNUM_OK;
-  std::vector<float2> h_img;
-  cudaError_t e = cudaMalloc(&d_rf, rf_count * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&d_img, nimg * sizeof(float2));
-  if (e == cudaSuccess && w) e = cudaMalloc(&d_w, nvox * sizeof(float));
-  if (e == cudaSuccess && w2) e = cudaMalloc(&d_w2, nvox * sizeof(float));
-  if (e == cudaSuccess) e = cudaMemcpy(d_rf, rf, rf_count * sizeof(double), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) {
-    s = cuda_status(e);
-    goto done;
+  if (!P->h_rf) {
+    if ((s = P->alloc(&P->h_rf, rf_count)) || (P->blas && (s = P->alloc(&P->h_rf32, rf_count))) ||
+        (s = P->alloc(&P->h_img, nimg)) || (s = P->alloc(&P->h_planes, 2 * nimg)) ||
+        (s = P->alloc(&P->h_w, nvox)) || (s = P->alloc(&P->h_w2, nvox)))
+      return s;
+    P->h_rf_count = rf_count;
   }
+  if (rf_count != P->h_rf_count) return FNUM_ERR_ARGUMENT;
+  float* d_w = w ? P->h_w : nullptr;
+  float* d_w2 = w2 ? P->h_w2 : nullptr;
+  cudaError_t e = cudaMemcpy(P->h_rf, rf, rf_count * sizeof(double), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_status(e);
   if (P->blas) {
-    // float RF for the GEMM band DFT (the first half of a second buffer's worth of the doubles)
-    e = cudaMalloc(&d_rf32, rf_count * sizeof(float));
-    if (e == cudaSuccess) e = fnum::launch_to_float(d_rf, d_rf32, rf_count, 0);
-    if (e != cudaSuccess) {
-      s = cuda_status(e);
-      goto done;
-    }
-    if ((s = plan_dft(P, d_rf32, 0, 0))) goto done;
-  } else if ((s = plan_dft(P, d_rf, 1, 0))) {
-    goto done;
+    // float RF for the GEMM band DFT
+    if ((e = fnum::launch_to_float(P->h_rf, P->h_rf32, rf_count, 0)) != cudaSuccess) return cuda_status(e);
+    if ((s = plan_dft(P, P->h_rf32, 0, 0))) return s;
+  } else if ((s = plan_dft(P, P->h_rf, 1, 0))) {
+    return s;
   }
-  if ((s = plan_beamform(P, d_img, d_w, d_w2, 0))) goto done;
-  h_img.resize(nimg);
-  e = cudaMemcpy(h_img.data(), d_img, nimg * sizeof(float2), cudaMemcpyDeviceToHost);
+  if ((s = plan_beamform(P, P->h_img, d_w, d_w2, 0))) return s;
+  if ((e = fnum::launch_split_complex(P->h_img, nimg, P->h_planes, P->h_planes + nimg, 0)) != cudaSuccess)
+    return cuda_status(e);
+  e = cudaMemcpy(re, P->h_planes, nimg * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(im, P->h_planes + nimg, nimg * sizeof(float), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && w) e = cudaMemcpy(w, d_w, nvox * sizeof(float), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && w2) e = cudaMemcpy(w2, d_w2, nvox * sizeof(float), cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) {
-    s = cuda_status(e);
-    goto done;
-  }
-  {
-    unsigned long long c[8];
-    e = cudaMemcpy(c, P->counters, sizeof(c), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) {
-      s = cuda_status(e);
-      goto done;
-    }
-    if (c[2] & fnum::ERR_SEG_OVERFLOW) {
-      s = FNUM_ERR_INTERNAL;
-      goto done;
-    }
-  }
-  for (size_t v = 0; v < nimg; ++v) {
-    re[v] = h_img[v].x;
-    im[v] = h_img[v].y;
-  }
-done:
-  if (d_rf) cudaFree(d_rf);
-  if (d_rf32) cudaFree(d_rf32);
-  if (d_img) cudaFree(d_img);
-  if (d_w) cudaFree(d_w);
-  if (d_w2) cudaFree(d_w2);
-  (void)cudaGetLastError();
-  return s;
+  if (e != cudaSuccess) return cuda_status(e);
+  unsigned long long c[8];
+  if ((e = cudaMemcpy(c, P->counters, sizeof(c), cudaMemcpyDeviceToHost)) != cudaSuccess) return cuda_status(e);
+  if (c[2] & fnum::ERR_SEG_OVERFLOW) return FNUM_ERR_INTERNAL;
+  return FNUM_OK;
 }
 
 // one cached plan per gateway: repeated calls with the same arguments reuse

@@ -126,6 +126,7 @@ cudaError_t launch_dft_sa(const void* rf, int is_double, int nsig, int nt, const
 cudaError_t launch_dft_matrix(const float2* tw, int N, int nt, int k_lb, int K, float* W, cudaStream_t s);
 cudaError_t launch_dft_scatter_pw(const float2* C, int na, int ne, int K, float2* X, cudaStream_t s);
 cudaError_t launch_to_float(const double* in, float* out, size_t n, cudaStream_t s);
+cudaError_t launch_split_complex(const float2* in, size_t n, float* re, float* im, cudaStream_t s);
 int pw_fused_grid(const PWDev& d, int* blocks_per_sm);   // grid of d's variant, all blocks resident
 int pw_fused_max_grid(const PWDev& d);                     // largest of those over the variants
 int pw_variant_count();

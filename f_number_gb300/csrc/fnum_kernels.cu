@@ -326,6 +326,20 @@ cudaError_t launch_dft_scatter_pw(const float2* C, int na, int ne, int K, float2
   return cudaGetLastError();
 }
 
+// complex image -> separate real and imaginary planes (the MEX output layout)
+__global__ void split_complex_kernel(const float2* __restrict__ in, size_t n, float* __restrict__ re,
+                                     float* __restrict__ im) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float2 v = in[i];
+    re[i] = v.x;
+    im[i] = v.y;
+  }
+}
+cudaError_t launch_split_complex(const float2* in, size_t n, float* re, float* im, cudaStream_t s) {
+  split_complex_kernel<<<608, 256, 0, s>>>(in, n, re, im);
+  return cudaGetLastError();
+}
+
 __global__ void to_float_kernel(const double* __restrict__ in, float* __restrict__ out, size_t n) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     out[i] = (float)in[i];
@@ -1041,7 +1055,7 @@ pw_event_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
 // aperture data come from the segment lists through a table in shared memory
 // that lanes 0..15 of each warp fill ahead of the bins.
 constexpr int TC_WARPS = NTHREADS / 32;
-constexpr int TC_TB = 64;   // bins per flush and receive-phasor re-anchoring
+constexpr int TC_TB = 32;   // bins per flush and receive-phasor re-anchoring
 constexpr int TC_TT = 16;   // bins per aperture table
 
 __device__ __forceinline__ void tc_split(float x0, float x1, unsigned& hi, unsigned& lo) {
