@@ -26,6 +26,7 @@ ABI_VERSION = 3   # FNUM_ABI_VERSION of include/fnum.h
 # status codes (fnum_status)
 OK = 0
 ERR_NO_DEVICE = 1
+ERR_ARGUMENT = 18
 ERR_INTERNAL = 21
 ERR_NOALLOC_TOO_LARGE = 24
 ERR_M_ELEMENTS = 25

@@ -129,3 +129,13 @@ def test_no_device_is_reported(built_lib):
     with pytest.raises(FNumError) as e:
         gpu_bf_das_pw_rf(np.zeros(3), np.array([1e-3, 2e-3]), np.zeros((64, 8)), 20e6, 0.0, 2e-4, 3e-4, 1540.0)
     assert e.value.identifier == "gpu_bf_das_pw_rf:NoCUDADevices"
+
+
+def test_variant_and_peak_entry_points_check_arguments(built_lib):
+    """fnum_plan_set_kernel_variant and fnum_diag_mma_f16_peak refuse null arguments
+    before touching a device."""
+    from f_number_gb300 import _lib
+    L = _lib.lib()
+    assert L.fnum_plan_set_kernel_variant(None, 1) == _lib.ERR_ARGUMENT
+    assert L.fnum_diag_mma_f16_peak(0, None) == _lib.ERR_ARGUMENT
+    assert L.fnum_diag_fp32_peak(0, None) == _lib.ERR_ARGUMENT
