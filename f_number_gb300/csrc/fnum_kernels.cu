@@ -525,6 +525,11 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
+// asynchronous 4-byte global -> shared copy
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
@@ -1987,13 +1992,38 @@ sa_fused_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
 // sa_fused_kernel with a boxcar receive window.
 constexpr int SA_EV_BINS = 32;
 
+// Issues the copy of one spectrum chunk for sa_event_kernel: per bin, chains in pairs
+// (2p, 2p+1) laid out {re_2p, re_2p+1, im_2p, im_2p+1}, so one 16-byte load feeds the
+// packed recurrence of a pair.
+template <int EPT>
+__device__ __forceinline__ void sa_stage_chunk_pairs(float* dst, const SADev& d, int t, int r0, int kc_lo, int nk,
+                                                     int tid, const float2* X) {
+  constexpr int ROW = 2 * EPT;
+  for (int idx = tid; idx < KCHUNK * EPT; idx += NTHREADS) {
+    const int kk = idx % KCHUNK, q = idx / KCHUNK;
+    const int r = r0 + q;
+    if (kk >= nk) continue;
+    float* o = &dst[kk * ROW + 4 * (q >> 1) + (q & 1)];
+    if (r < d.ne) {
+      const float* src = reinterpret_cast<const float*>(&X[((size_t)t * d.ne + r) * d.K + (kc_lo - d.k_lb + kk)]);
+      cp_async4(o, src);
+      cp_async4(o + 2, src + 1);
+    } else {
+      o[0] = 0.0f;
+      o[2] = 0.0f;
+    }
+  }
+  cp_async_commit();
+}
+
 template <int EPT, int WT>
 __global__ void __launch_bounds__(NTHREADS, 4)
 sa_event_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ wtx_out, float* __restrict__ wrx_out,
                 int n_tiles_x, int n_tiles_z, int weights_only) {
-  static_assert(EPT <= 31, "receive mask");
-  constexpr int ROW = (EPT + 1) & ~1;
-  __shared__ __align__(16) float2 xs[2][KCHUNK * ROW];
+  static_assert(EPT <= 31 && EPT % 2 == 0, "receive mask, chain pairs");
+  constexpr int NP = EPT / 2;     // chains are processed in pairs by packed FP32x2 instructions
+  constexpr int ROW = 2 * EPT;    // floats per bin: per pair {re, re, im, im}
+  __shared__ __align__(16) float xs[2][KCHUNK * ROW];
   __shared__ float2 ev[SA_EV_BINS][NTHREADS];        // {f from the bin on, receive mask}
   __shared__ int ranges[4];
   __shared__ int s_tile;
@@ -2072,13 +2102,30 @@ sa_event_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
           const int hi = min(max(code_iub(rcode), emid - 1), m_hi_cap);
           return (lo <= hi) ? ((2u << (hi - r0)) - (1u << (lo - r0))) : 0u;
         };
-        float2 z[EPT], A[EPT];
+        // per pair of chains: accumulators {re, re}, {im, im} and steps {re, re}, {im, im}, {-im, -im}
+        float2 AR[NP], AI[NP], ZR[NP], ZI[NP], NZI[NP];
 #pragma unroll
-        for (int q = 0; q < EPT; ++q) {
-          const int e = min(r0 + q, d.ne - 1);
-          z[q] = cis_ku(1, df_add(df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2)), utx));
-          A[q] = make_float2(0.0f, 0.0f);
+        for (int p = 0; p < NP; ++p) {
+          const float2 z0 = cis_ku(1, df_add(df_sqrt(df_add(df_sqr(df_sub(d.el_u[min(r0 + 2 * p, d.ne - 1)], xu)), zu2)), utx));
+          const float2 z1 =
+              cis_ku(1, df_add(df_sqrt(df_add(df_sqr(df_sub(d.el_u[min(r0 + 2 * p + 1, d.ne - 1)], xu)), zu2)), utx));
+          ZR[p] = make_float2(z0.x, z1.x);
+          ZI[p] = make_float2(z0.y, z1.y);
+          NZI[p] = make_float2(-z0.y, -z1.y);
+          AR[p] = AI[p] = make_float2(0.0f, 0.0f);
         }
+        auto getA = [&](int q) -> float2 {
+          return (q & 1) ? make_float2(AR[q >> 1].y, AI[q >> 1].y) : make_float2(AR[q >> 1].x, AI[q >> 1].x);
+        };
+        auto setA = [&](int q, float2 v) {
+          if (q & 1) {
+            AR[q >> 1].y = v.x;
+            AI[q >> 1].y = v.y;
+          } else {
+            AR[q >> 1].x = v.x;
+            AI[q >> 1].x = v.y;
+          }
+        };
         // segment in effect at kt, and the state of the boundary pre-pass:
         // tx code and tx window value of the last resolved entry
         int s = 0;
@@ -2098,15 +2145,16 @@ sa_event_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
         float2 part = make_float2(0.0f, 0.0f);
         const int c_top = (kt - d.k_lb) / KCHUNK;
         __syncthreads();  // every thread is done with both buffers of the previous pass
-        sa_stage_chunk<EPT>(xs[0], d, t, r0, d.k_lb + c_top * KCHUNK, kt - (d.k_lb + c_top * KCHUNK) + 1, tid, Xsrc);
+        sa_stage_chunk_pairs<EPT>(xs[0], d, t, r0, d.k_lb + c_top * KCHUNK, kt - (d.k_lb + c_top * KCHUNK) + 1, tid,
+                                  Xsrc);
         int buf = 0;
         for (int chunk = c_top; chunk >= 0; --chunk) {
           const int kc_lo = d.k_lb + chunk * KCHUNK;
           const int kc_hi = (chunk == c_top) ? kt : kc_lo + KCHUNK - 1;
           cp_async_wait_all();
           __syncthreads();
-          if (chunk > 0) sa_stage_chunk<EPT>(xs[buf ^ 1], d, t, r0, kc_lo - KCHUNK, KCHUNK, tid, Xsrc);
-          const float2* xb = xs[buf];
+          if (chunk > 0) sa_stage_chunk_pairs<EPT>(xs[buf ^ 1], d, t, r0, kc_lo - KCHUNK, KCHUNK, tid, Xsrc);
+          const float* xb = xs[buf];
           buf ^= 1;
           for (int ks_hi = kc_hi; ks_hi >= kc_lo; ks_hi -= SA_EV_BINS) {
             const int ks_lo = max(kc_lo, ks_hi - (SA_EV_BINS - 1));
@@ -2139,7 +2187,7 @@ sa_event_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
                   for (int q = 0; q < EPT; ++q) {
                     if ((leave >> q) & 1u) {
                       const dfl u = df_add(df_sqrt(df_add(df_sqr(df_sub(d.el_u[r0 + q], xu)), zu2)), utx);
-                      const float2 tt = cmul(cis_ku(k + 1, u), A[q]);
+                      const float2 tt = cmul(cis_ku(k + 1, u), getA(q));
                       part.x = fmaf(f, tt.x, part.x);
                       part.y = fmaf(f, tt.y, part.y);
                     }
@@ -2147,17 +2195,18 @@ sa_event_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
                 }
                 const float r = stay ? __fdividef(f, fn) : 0.0f;
                 if (stay == m && mn == m) {
+                  const float2 rr = make_float2(r, r);
 #pragma unroll
-                  for (int q = 0; q < EPT; ++q) {
-                    A[q].x *= r;
-                    A[q].y *= r;
+                  for (int p = 0; p < NP; ++p) {
+                    AR[p] = __fmul2_rn(AR[p], rr);
+                    AI[p] = __fmul2_rn(AI[p], rr);
                   }
                 } else {
 #pragma unroll
                   for (int q = 0; q < EPT; ++q) {
                     const bool st = (stay >> q) & 1u;
-                    A[q].x = st ? A[q].x * r : 0.0f;
-                    A[q].y = st ? A[q].y * r : 0.0f;
+                    const float2 a = getA(q);
+                    setA(q, make_float2(st ? a.x * r : 0.0f, st ? a.y * r : 0.0f));
                   }
                 }
                 f = fn;
@@ -2165,13 +2214,15 @@ sa_event_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
                 emask &= ~(1u << (k - ks_lo));
                 nev = emask ? ks_lo + 31 - __clz(emask) : -1;
               }
-              const float2* xr = &xb[(k - kc_lo) * ROW];
+              const float4* xr = reinterpret_cast<const float4*>(&xb[(k - kc_lo) * ROW]);
+              // A <- A z + x per chain, two chains per packed instruction (the same fused
+              // operations as fmaf(Ax, zx, fmaf(-Ay, zy, xr)), fmaf(Ax, zy, fmaf(Ay, zx, xi)))
 #pragma unroll
-              for (int q = 0; q < EPT; ++q) {
-                const float2 x = xr[q];
-                const float2 Aq = A[q], zq = z[q];
-                A[q].x = fmaf(Aq.x, zq.x, fmaf(-Aq.y, zq.y, x.x));
-                A[q].y = fmaf(Aq.x, zq.y, fmaf(Aq.y, zq.x, x.y));
+              for (int p = 0; p < NP; ++p) {
+                const float4 xv = xr[p];
+                const float2 ar = AR[p], ai = AI[p];
+                AR[p] = __ffma2_rn(ar, ZR[p], __ffma2_rn(ai, NZI[p], make_float2(xv.x, xv.y)));
+                AI[p] = __ffma2_rn(ar, ZI[p], __ffma2_rn(ai, ZR[p], make_float2(xv.z, xv.w)));
               }
             }
           }
@@ -2180,12 +2231,13 @@ sa_event_kernel(const SADev d, float2* __restrict__ image, float* __restrict__ w
             for (int q = 0; q < EPT; ++q) {
               if ((m >> q) & 1u) {
                 const dfl u = df_add(df_sqrt(df_add(df_sqr(df_sub(d.el_u[r0 + q], xu)), zu2)), utx);
-                const float2 tt = cmul(cis_ku(kc_lo, u), A[q]);
+                const float2 tt = cmul(cis_ku(kc_lo, u), getA(q));
                 part.x = fmaf(f, tt.x, part.x);
                 part.y = fmaf(f, tt.y, part.y);
               }
-              A[q] = make_float2(0.0f, 0.0f);
             }
+#pragma unroll
+            for (int p = 0; p < NP; ++p) AR[p] = AI[p] = make_float2(0.0f, 0.0f);
           }
         }
         float y = part.x - comp.x, tt = acc.x + y;
