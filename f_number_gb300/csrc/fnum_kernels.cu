@@ -3,12 +3,19 @@
 // Stages (reference counterparts in the f_number project):
 //   twiddles_kernel      table e^{-2 pi i m / N}, m < N (FP64 sincospi, rounded to float)
 //   dft_band_kernel      RF -> band spectra, only bins k_lb..k_ub
-//                        (replaces cufftPlan1d/cufftExecR2C, +cuda/gpu_bf_das_pw_rf.cu:917-925)
+//                        (replaces cufftPlan1d/cufftExecR2C, +cuda/gpu_bf_das_pw_rf.cu:917-925);
+//                        float RF goes through one SGEMM against dft_matrix_kernel's
+//                        twiddle matrix instead (host side)
 //   pw_fused_kernel      one voxel per thread; replaces das_kernel_distances_pw,
 //                        das_kernel_phase_shifts, the per-bin cublasCgemm and
 //                        das_kernel_normalization (+cuda/gpu_bf_das_pw_rf.cu:965-1057)
-//   sa_fused_kernel      the same for synthetic-aperture data
+//   pw_event_kernel      the same recurrence with the segment boundaries resolved ahead
+//                        of the bin loop
+//   pw_tc_kernel         the same image from per-bin [voxels x elements] . [elements x
+//                        angles] products on the tensor cores (mma.sync, fp16 hi/lo)
+//   sa_fused_kernel      the recurrence for synthetic-aperture data
 //                        (+cuda/gpu_bf_saft_rf.cu:1144-1201, saft_kernel_phase_shifts.cu)
+//   sa_event_kernel      the same for a boxcar receive window, boundaries resolved ahead
 //   pw_plain_kernel / sa_plain_kernel
 //                        one voxel per thread with the reference's FP32 arithmetic per term
 //                        (__sincosf, float geometry): the plain drop-in baseline.
