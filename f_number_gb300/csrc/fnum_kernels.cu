@@ -1064,8 +1064,8 @@ pw_event_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
 // the exact phase at the end of every TC_TB bins, where the receive phasors
 // r^k are also re-anchored exactly.  The weights b enter R bin by bin, so a
 // segment boundary costs nothing in the recurrence: the per-(voxel, bin)
-// aperture data come from the segment lists through a table in shared memory
-// that lanes 0..15 of each warp fill ahead of the bins.
+// aperture data (inverse half-widths, 1/W) come from the segment lists through a
+// table in shared memory that lanes 0..15 of each warp fill ahead of the bins.
 constexpr int TC_WARPS = NTHREADS / 32;
 constexpr int TC_TB = 32;   // bins per flush and receive-phasor re-anchoring
 constexpr int TC_TT = 16;   // bins per aperture table
@@ -1147,7 +1147,7 @@ __global__ void __launch_bounds__(256) tc_prep_kernel(const PWDev d, int n_ap) {
 template <int WIN>
 __global__ void __launch_bounds__(NTHREADS, 4)
 pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weights, int n_tiles_x, int n_tiles_z) {
-  __shared__ float4 apt[TC_WARPS][TC_TT][16];   // {lo | (hi+1) << 16, 1/L_left, 1/L_right, 1/W} per bin, voxel
+  __shared__ float4 apt[TC_WARPS][TC_TT][16];   // {-, 1/L_left, 1/L_right, 1/W} per bin, voxel
   __shared__ int e_range[2];
   __shared__ int s_tile;
   __shared__ int s_nseg[TC_WARPS * 16];
@@ -1220,24 +1220,25 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
     const int4* bseg = seg_blk + (size_t)bv * d.seg_cap;
     const int bnseg = s_nseg[bv];
     const dfl bxm = d.col_m[min(tx * TC_TILE_X + (bv >> 5), d.nx - 1)];
-    const int bemid = d.col_emid[min(tx * TC_TILE_X + (bv >> 5), d.nx - 1)];
     auto entry_of = [&](int4 c) -> float4 {
       const int ilb = code_ilb(c.y), iub = code_iub(c.y);
-      const int lo = min(ilb, bemid), hi = max(iub, bemid - 1);
-      // a side whose half-width is not positive holds no element of the aperture;
-      // its 0 keeps the other side's elements (distance 0 on this side) finite
-      float il = 0.0f, ir = 0.0f;
+      // An element is in the aperture exactly when its window argument u = d / L is
+      // below 1: the nearest element outside lies (pitch - width/2) / L beyond it, the
+      // outermost inside width/2 / L within.  A side without aperture (no edge element,
+      // or a half-width that is not positive) gets 1/L = 1e30, which sends its elements
+      // to u >= 1 and keeps the other side's (distance 0 on this side) at u = d / L.
+      float il = 1.0e30f, ir = 1.0e30f;
       if (ilb < d.ne) {
         const dfl l = lb_s[ilb];
         const float L = (bxm.x - l.x) + (bxm.y - l.y);
-        il = (L > 0.0f) ? __fdividef(1.0f, L) : 0.0f;
+        if (L > 0.0f) il = __fdividef(1.0f, L);
       }
       if (iub >= 0) {
         const dfl u = ub_s[iub];
         const float L = (u.x - bxm.x) + (u.y - bxm.y);
-        ir = (L > 0.0f) ? __fdividef(1.0f, L) : 0.0f;
+        if (L > 0.0f) ir = __fdividef(1.0f, L);
       }
-      return make_float4(__int_as_float(lo | ((hi + 1) << 16)), il, ir, __int_as_float(c.z));
+      return make_float4(0.0f, il, ir, __int_as_float(c.z));
     };
     s_acc[0][tid] = s_acc[1][tid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 
@@ -1285,7 +1286,7 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
         // builder state: the segment in effect and the next entry
         if (lane < 16) {
           int bs = 0;
-          float4 bent = make_float4(__int_as_float(d.ne), 0.0f, 0.0f, 0.0f);  // lo = ne, hi = -1: empty
+          float4 bent = make_float4(0.0f, 1.0e30f, 1.0e30f, 0.0f);  // empty aperture
           int4 bnext = make_int4(-1, 0, 0, 0);
           if (bnseg > 0) {
             bs = seg_find1(bseg, bnseg, kt);
@@ -1361,15 +1362,12 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
                 float2 rre[2], rim[2];
 #pragma unroll
                 for (int V = 0; V < 2; ++V) {
-                  const int lohi = __float_as_int(en[V].x);
-                  const int lo = lohi & 0xffff, hi = (lohi >> 16) - 1;
                   float b[2];
 #pragma unroll
                   for (int i = 0; i < 2; ++i) {
-                    const int e = e0 + 8 * s + 2 * q + i;
                     const float2 dlr = s_dx[2 * TC_KS * V + 2 * s + i][tid];
-                    const float w = win_t<WIN>(d.window_par, inv_par, fmaf(dlr.x, en[V].y, dlr.y * en[V].z));
-                    b[i] = (e >= lo && e <= hi) ? w * en[V].w : 0.0f;
+                    const float u = fmaf(dlr.x, en[V].y, dlr.y * en[V].z);
+                    b[i] = (u < 1.0f) ? win_t<WIN>(d.window_par, inv_par, u) * en[V].w : 0.0f;
                   }
                   // R = b r^k and r^k <- r^k conj(r), two elements per packed FP32 instruction
                   const float2 bb = make_float2(b[0], b[1]);
