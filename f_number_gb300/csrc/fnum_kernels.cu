@@ -1224,7 +1224,8 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
       const int ilb = code_ilb(c.y), iub = code_iub(c.y);
       // An element is in the aperture exactly when its window argument u = d / L is
       // below 1: the nearest element outside lies (pitch - width/2) / L beyond it, the
-      // outermost inside width/2 / L within.  A side without aperture (no edge element,
+      // outermost inside width/2 / L within (pitch > width is checked at plan creation;
+      // the margin exceeds the FP32 rounding of u for any width above 1e-6 of L).  A side without aperture (no edge element,
       // or a half-width that is not positive) gets 1/L = 1e30, which sends its elements
       // to u >= 1 and keeps the other side's (distance 0 on this side) at u = d / L.
       float il = 1.0e30f, ir = 1.0e30f;
