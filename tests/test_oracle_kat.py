@@ -245,3 +245,33 @@ def test_sharpness_gradient_oracle_matches_finite_differences():
     eps = 1e-5                                 # relative to the RF's ~0.13 rms (central differences, error ~eps^2)
     fd = (run(rf + eps * d_rf, 1540.0)[0] - run(rf - eps * d_rf, 1540.0)[0]) / (2 * eps)
     assert abs(fd - an) <= 1e-6 * abs(an)
+
+
+def test_saft_transmit_receive_symmetry_identity():
+    """The identity behind the SAFT kernels' symmetric path, in FP64: with equal transmit
+    and receive windows, F-numbers and normalisations, beamforming RF' with
+    RF'[t][r] = RF[t][r] + RF[r][t] (t < r), RF'[t][t] = RF[t][t], RF'[t][r] = 0 (t > r)
+    gives the image of RF (the band DFT is linear and pair (t, r) has the weight and
+    phase of (r, t)).  With unequal F-numbers it does not."""
+    rng = np.random.default_rng(17)
+    ne, nt = 10, 200
+    rf = rng.standard_normal((ne, ne, nt))                   # [tx, rx, t], not reciprocal
+    sym = np.zeros_like(rf)
+    for t in range(ne):
+        sym[t, t] = rf[t, t]
+        for r in range(t + 1, ne):
+            sym[t, r] = rf[t, r] + rf[r, t]
+    px = np.linspace(-1e-3, 1e-3, 5)
+    pz = np.linspace(3e-3, 6e-3, 4)
+    fn = {"kind": "directivity", "width_over_pitch": 0.918, "obliquity": "soft", "attenuation_dB": 3.0}
+    other = {"kind": "constant", "value": 1.2}
+    for wt, ftx, equal in ((("hann", 0.0), fn, True), (("boxcar", 0.0), fn, True), (("boxcar", 0.0), other, False)):
+        a = O.das_sa_mex(px, pz, np.transpose(rf, (2, 1, 0)), 40e6, 0.918 * 0.3e-3, 0.3e-3, 1540.0, (2e6, 9e6), 0.0,
+                         wt, wt, ftx, fn, "on", "on")[0]
+        b = O.das_sa_mex(px, pz, np.transpose(sym, (2, 1, 0)), 40e6, 0.918 * 0.3e-3, 0.3e-3, 1540.0, (2e6, 9e6), 0.0,
+                         wt, wt, ftx, fn, "on", "on")[0]
+        rel = np.linalg.norm(a - b) / np.linalg.norm(a)
+        if equal:
+            assert rel < 1e-12, (wt, rel)
+        else:
+            assert rel > 1e-3, (wt, rel)
