@@ -195,6 +195,20 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def replica_throughput(total_ms, steps, dist=None, device=None):
+    """Whole-job frames/s of replicas: each of the world's ranks processed `steps`
+    frames of its own, and the job took as long as its slowest rank (max over ranks
+    of the timed region).  Returns (frames/s, ms per step of the slowest rank)."""
+    world = 1
+    if dist is not None:
+        import torch
+        world = dist.get_world_size()
+        t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return steps * world / (total_ms * 1e-3), total_ms / steps
+
+
 def run_ours(args):
     import torch
     from f_number_gb300 import _lib, das
@@ -241,15 +255,8 @@ def run_ours(args):
     step_ms = [a.elapsed_time(c) for a, b, c in evs]
     dft_ms = [a.elapsed_time(b) for a, b, c in evs]
     bf_ms = [b.elapsed_time(c) for a, b, c in evs]
-    total_ms = float(sum(step_ms))
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    value, ms_per_step = replica_throughput(float(sum(step_ms)), args.steps, dist, dev)
     info = plan.info()
-    frames = args.steps * world
-    value = frames / (total_ms * 1e-3)
-    ms_per_step = total_ms / args.steps
 
     # end to end through the public API: pinned host RF (double, MATLAB layout) in, host image out
     e2e = None
