@@ -30,7 +30,7 @@ def test_replica_throughput_two_gloo_ranks():
     torch = pytest.importorskip("torch")
     import torch.multiprocessing as mp
     world = 2
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()     # no fork of a multi-threaded process
     mp.spawn(_rank, args=(world, _free_port(), out), nprocs=world, join=True)
     for r in range(world):
         value, ms = out[r]
