@@ -50,6 +50,8 @@ def parse():
                     "geometry with RF simulated at 1500 m/s")
     ap.add_argument("--frames", type=int, default=64, help="batch: frames per batch")
     ap.add_argument("--no-autotune", action="store_true", help="batch: keep each plan's default kernel variant")
+    ap.add_argument("--variant", type=int, default=0,
+                    help="cpwc: pin the plane-wave kernel variant (fnum_plan_set_kernel_variant; 0 = the default)")
     ap.add_argument("--band", default="full", choices=["full", "2-7"],
                     help="saft band: the gateway default [DBL_MIN, f_s/2] or 2-7 MHz")
     return ap.parse_args()
@@ -225,6 +227,8 @@ def run_ours(args):
     plan = das.PWPlan(wl.positions_x, wl.positions_z, wl.n_samples, wl.array.n_elements, wl.f_s, wl.angles,
                       wl.array.width, wl.array.pitch, wl.c, list(wl.f_bounds), 0.0, win, fn, device=local,
                       compound=True, kernel=args.kernel)
+    if args.variant and args.kernel == "fused":
+        plan.set_kernel_variant(args.variant)
     rf = torch.tensor(wl.rf, dtype=torch.float32, device=dev)                 # [A, E, T]
     img = torch.empty((1, plan.n_x, plan.n_z), dtype=torch.complex64, device=dev)
     wts = torch.empty((plan.n_x, plan.n_z), dtype=torch.float32, device=dev)
