@@ -8,7 +8,11 @@ recording is not distributed).  One step = one compounded frame: band DFT of
 the 11 x 128 RF lines and the fused beamformer, inputs resident in HBM.
 
 Prints one JSON line.  ``--impl reference`` times the reference's CPU path
-(das_pw.m, restated in C with OpenMP under oracle/) on the host cores instead.
+(das_pw.m, restated in C with OpenMP under oracle/) on the host cores instead;
+on the 11-angle frame it times a bounded random sample of voxels and says so in
+its ``extrapolated`` field.  ``--workload pw1`` (single 0 deg plane wave,
+256 x 256, Tukey(0.5), 2.25-6.75 MHz) is small enough for both arms to time
+complete frames; the headline line carries that comparison as ``cfg1_anchor``.
 """
 from __future__ import annotations
 
@@ -27,6 +31,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "CPWC frames/s (11 angles, 512x512, 128 el)"
+PW1_METRIC = "PW frames/s (1 angle, 256x256, 128 el)"
 UNIT = "frames/s"
 L2_FLUSH_BYTES = 512 << 20          # > 129 MB L2
 
@@ -43,8 +48,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--grid", type=int, default=512, help="voxels per side (512 = the benchmark grid; smaller "
                     "sizes keep the same 0.06 mm spacing, for profiling)")
-    ap.add_argument("--workload", default="cpwc", choices=["cpwc", "saft", "batch", "adjoint"],
-                    help="cpwc (default, the headline); saft: 128 x 128 synthetic aperture, 3072 samples at "
+    ap.add_argument("--workload", default="cpwc", choices=["cpwc", "pw1", "saft", "batch", "adjoint"],
+                    help="cpwc (default, the headline); pw1: single 0 deg plane wave, 256 x 256, whole frames "
+                    "on both arms; saft: 128 x 128 synthetic aperture, 3072 samples at "
                     "40 MHz, 400 x 400 voxels, directivity F-number, boxcar windows; batch: 64 plane-wave frames "
                     "of uneven shape in one CUDA graph; adjoint: sharpness-loss gradients (dL/dc, dL/dX*) of the cpwc "
                     "geometry with RF simulated at 1500 m/s")
@@ -63,8 +69,19 @@ def workload(grid=512):
     return wl, windows.hann(), f_numbers.grating.angle_lb(60.0, 1.5)
 
 
+def workload_pw1(grid=256):
+    from f_number_gb300 import f_numbers, synth, windows
+    wl = synth.pw_single_angle(seed=0, grid=(grid, grid))
+    return wl, windows.tukey(0.5), f_numbers.grating.angle_lb(60.0, 1.5)
+
+
 def config_of(wl, kernel):
     g = "%dx%d" % (wl.positions_x.size, wl.positions_z.size)
+    if wl.angles.size == 1:
+        return {"workload": "pw_1angle_128el_2048smp_%s_2.25-6.75MHz_tukey0.5_anglelb60" % g,
+                "n_angles": 1, "n_elements": wl.array.n_elements, "n_samples": wl.n_samples,
+                "grid": [int(wl.positions_x.size), int(wl.positions_z.size)], "band_hz": list(wl.f_bounds),
+                "kernel": kernel, "l2": "flushed between timed steps (512 MB write)", "data": "synthetic seeded RF"}
     return {"workload": "cpwc_11angles_128el_2048smp_%s_2-7MHz_hann_anglelb60" % g,
             "n_angles": int(wl.angles.size), "n_elements": wl.array.n_elements, "n_samples": wl.n_samples,
             "grid": [int(wl.positions_x.size), int(wl.positions_z.size)], "band_hz": list(wl.f_bounds),
@@ -75,6 +92,9 @@ def config_of(wl, kernel):
 # CPU baseline: das_pw.m restated in C (oracle), bounded sample of voxels
 # ---------------------------------------------------------------------------
 def cpu_das_pw_m(wl, win, fn, seconds, threads=0):
+    """das_pw.m CPU semantics on a bounded random sample of the frame's voxels,
+    scaled to the frame (the per-voxel cost is nearly uniform).  Returns
+    (frames/s, cpu_baseline dict with an ``extrapolated`` record)."""
     from oracle import coracle as CO
     nx, nz = wl.positions_x.size, wl.positions_z.size
     rng = np.random.default_rng(123)
@@ -98,8 +118,53 @@ def cpu_das_pw_m(wl, win, fn, seconds, threads=0):
     t = run(n)
     fps = n / (t * n_vox)
     return fps, {"value": fps, "unit": UNIT, "cores": th, "kind": "port",
-                 "sample": "das_pw.m CPU semantics (oracle/fnum_oracle.c) on %d random voxels x 11 angles "
-                           "(%.1f s incl. FFT), scaled to the %d-voxel frame" % (n, t, n_vox)}
+                 "sample": "das_pw.m CPU semantics (oracle/fnum_oracle.c) on %d random voxels x %d angles "
+                           "(%.1f s incl. FFT), scaled to the %d-voxel frame" % (n, wl.angles.size, t, n_vox),
+                 "extrapolated": {"voxels": int(n), "of": int(n_vox), "seconds": t}}
+
+
+def cpu_whole_frame(wl, win, fn, threads=0):
+    """das_pw.m CPU semantics over every voxel of the frame (no extrapolation).
+    Returns (frames/s, seconds)."""
+    from oracle import coracle as CO
+    nx, nz = wl.positions_x.size, wl.positions_z.size
+    ix, iz = np.meshgrid(np.arange(nx), np.arange(nz), indexing="ij")
+    th = threads or CO.max_threads()
+    t = time.perf_counter()
+    CO.pw_m(wl.positions_x, wl.positions_z, wl.rf, wl.f_s, wl.angles, wl.array.width, wl.array.pitch, wl.c,
+            wl.f_bounds, 0.0, win.spec(), fn.spec(), "on", ix.ravel(), iz.ravel(), threads=th)
+    dt = time.perf_counter() - t
+    return 1.0 / dt, dt, th
+
+
+def accuracy_of(wl, win, fn, img, n_random=192, n_bright=64):
+    """Error of a compounded frame (img: [n_x, n_z] complex, scaled like the MEX)
+    against the FP64 oracle (MEX semantics, oracle/fnum_oracle.c) on a fixed
+    sample of voxels: n_random seeded random ones plus the n_bright brightest
+    of the frame.  The RF is the float32 RF the GPU beamformed."""
+    from oracle import coracle as CO
+    nx, nz = img.shape
+    rng = np.random.default_rng(7)
+    flat = np.abs(img).ravel()
+    pick = np.unique(np.concatenate([rng.choice(nx * nz, n_random, replace=False),
+                                     np.argsort(flat)[-n_bright:]]))
+    ix, iz = pick // nz, pick % nz
+    rf32 = np.asarray(wl.rf, dtype=np.float32).astype(np.float64)
+    ref, _, _ = CO.pw_mex(wl.positions_x, wl.positions_z, rf32, wl.f_s, wl.angles, wl.array.width, wl.array.pitch,
+                          wl.c, wl.f_bounds, 0.0, win.spec(), fn.spec(), "on", ix, iz)
+    got = img[ix, iz].astype(np.complex128)
+    thr = flat.max() * 10 ** (-40 / 20)
+    hi = np.abs(ref) > thr
+    dphi = np.abs(np.angle(got[hi] * np.conj(ref[hi])))
+    ddb = np.abs(20 * np.log10(np.abs(got[hi]) / np.abs(ref[hi])))
+    return {"rel_l2": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+            "max_phase_err_rad": float(dphi.max()) if dphi.size else None,
+            "max_bmode_db_err": float(ddb.max()) if ddb.size else None,
+            "voxels": int(pick.size), "voxels_above_-40dB": int(hi.sum()),
+            "against": "FP64 oracle (MEX semantics, oracle/fnum_oracle.c) on the float32 RF of the timed frame",
+            "sample": "%d seeded random voxels + the %d brightest of the frame" % (n_random, n_bright),
+            "bmode": "20 |log10(|I| / |I_ref|)| on voxels above -40 dB of the frame maximum (a common "
+                     "normaliser cancels)"}
 
 
 # ---------------------------------------------------------------------------
@@ -178,22 +243,46 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    wl, win, fn = workload(args.grid)
+    pw1 = args.workload == "pw1"
+    wl, win, fn = workload_pw1(256 if args.grid == 512 else args.grid) if pw1 else workload(args.grid)
     vals = []
     cb = None
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        cpu_das_pw_m(wl, win, fn, min(2.0, args.cpu_seconds / 4))
-    per = max(2.0, args.cpu_seconds / max(args.steps, 1))
-    for _ in range(args.steps):
-        fps, cb = cpu_das_pw_m(wl, win, fn, per)
-        vals.append(fps)
-    value = float(np.mean(vals))
-    cb["value"] = value
-    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+    if pw1:
+        # complete frames: every voxel of the 256 x 256 frame, each step
+        for _ in range(min(args.warmup, 1)):
+            cpu_whole_frame(wl, win, fn)
+        secs = []
+        for _ in range(args.steps):
+            fps, dt, th = cpu_whole_frame(wl, win, fn)
+            vals.append(fps)
+            secs.append(dt)
+        value = float(args.steps / sum(secs))
+        cb = {"value": value, "unit": UNIT, "cores": th, "kind": "port",
+              "sample": "das_pw.m CPU semantics (oracle/fnum_oracle.c), complete %dx%d frames"
+                        % (wl.positions_x.size, wl.positions_z.size)}
+        ms_per_step = 1e3 * sum(secs) / args.steps
+    else:
+        for _ in range(args.warmup if args.warmup < 1 else 1):
+            cpu_das_pw_m(wl, win, fn, min(2.0, args.cpu_seconds / 4))
+        per = max(2.0, args.cpu_seconds / max(args.steps, 1))
+        samples = []
+        for _ in range(args.steps):
+            fps, cb = cpu_das_pw_m(wl, win, fn, per)
+            vals.append(fps)
+            samples.append(cb["extrapolated"])
+        value = float(np.mean(vals))
+        cb["value"] = value
+        cb["extrapolated"] = {"voxels": int(sum(x["voxels"] for x in samples)), "of": samples[0]["of"],
+                              "seconds": float(sum(x["seconds"] for x in samples)), "steps": len(samples),
+                              "note": "each step times a random voxel sample and scales it to the frame"}
+        ms_per_step = 1e3 / value
+    out = {"impl": "reference", "metric": PW1_METRIC if pw1 else METRIC, "value": value, "unit": UNIT,
+           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": config_of(wl, "cpu"), "cpu_baseline": cb,
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if not pw1:
+        out["extrapolated"] = cb["extrapolated"]
     print(json.dumps(out))
 
 
@@ -223,7 +312,8 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    wl, win, fn = workload(args.grid)
+    pw1 = args.workload == "pw1"
+    wl, win, fn = workload_pw1(256 if args.grid == 512 else args.grid) if pw1 else workload(args.grid)
     plan = das.PWPlan(wl.positions_x, wl.positions_z, wl.n_samples, wl.array.n_elements, wl.f_s, wl.angles,
                       wl.array.width, wl.array.pitch, wl.c, list(wl.f_bounds), 0.0, win, fn, device=local,
                       compound=True, kernel=args.kernel)
@@ -257,7 +347,7 @@ def run_ours(args):
         dist.barrier()
     clk = clocks.stop()
     step_ms = [a.elapsed_time(c) for a, b, c in evs]
-    dft_ms = [a.elapsed_time(b) for a, b, c in evs]
+    dft_ms = [a.elapsed_time(b) for a, b, c in evs]    # operand split + tcgen05 GEMM
     bf_ms = [b.elapsed_time(c) for a, b, c in evs]
     value, ms_per_step = replica_throughput(float(sum(step_ms)), args.steps, dist, dev)
     info = plan.info()
@@ -320,24 +410,79 @@ def run_ours(args):
                           "peak_source": "measured mma.sync m16n8k16 f16/f32 throughput (fnum_diag_mma_f16_peak)"}
     if rank != 0:
         return
-    cb = None
+    acc = accuracy_of(wl, win, fn, img[0].cpu().numpy())
+    cb, anchor = None, None
     if not args.no_cpu:
-        _, cb = cpu_das_pw_m(wl, win, fn, args.cpu_seconds)
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        if pw1:
+            fps_cpu, dt_cpu, th = cpu_whole_frame(wl, win, fn)
+            cb = {"value": fps_cpu, "unit": UNIT, "cores": th, "kind": "port",
+                  "sample": "das_pw.m CPU semantics (oracle/fnum_oracle.c), one complete %dx%d frame (%.1f s)"
+                            % (wl.positions_x.size, wl.positions_z.size, dt_cpu)}
+        else:
+            _, cb = cpu_das_pw_m(wl, win, fn, args.cpu_seconds)
+            anchor = cfg1_anchor(args, local, dev, flush)
+    out = {"metric": PW1_METRIC if pw1 else METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32 (double-float phase)", "data": "synthetic",
            "config": config_of(wl, args.kernel),
            "gterms_per_s": info["terms"] / (ms_per_step * 1e-3) / 1e9,
            "stage_ms": {"band_dft": float(np.mean(dft_ms)), "beamform": bf_avg_ms},
-           "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "clocks": clk,
-           # per step: the band DFT is one cuBLAS SGEMM (a library launch) plus this library's
-           # reorder kernel; the beamformer adds the scale and fragment kernels for variant 9
-           "gpu_launches": args.steps * (4 if (args.kernel == "fused" and info["kernel_variant"] == 9) else 2),
-           "library_launches": {"cublasSgemm (band DFT)": args.steps}}
+           "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "clocks": clk, "accuracy": acc,
+           # per step: the band DFT (operand split + tcgen05 GEMM) and the beamformer, which adds
+           # the scale and fragment kernels for variant 9; no library kernels
+           "gpu_launches": args.steps * (5 if (args.kernel == "fused" and info["kernel_variant"] == 9) else 3),
+           "library_launches": {}}
+    if anchor is not None:
+        out["cfg1_anchor"] = anchor
     print(json.dumps(out))
     plan.close()
     if dist:
         dist.destroy_process_group()
+
+
+def cfg1_anchor(args, local, dev, flush, steps=10, warmup=3):
+    """The single-angle 256 x 256 frame (pw1) on both arms with complete frames:
+    GPU frames/s (device-timed, L2 flushed; and end to end through the gateway)
+    against the das_pw.m CPU semantics over every voxel of the frame."""
+    import torch
+    from f_number_gb300 import das
+    wl, win, fn = workload_pw1()
+    plan = das.PWPlan(wl.positions_x, wl.positions_z, wl.n_samples, wl.array.n_elements, wl.f_s, wl.angles,
+                      wl.array.width, wl.array.pitch, wl.c, list(wl.f_bounds), 0.0, win, fn, device=local,
+                      compound=True)
+    rf = torch.tensor(wl.rf, dtype=torch.float32, device=dev)
+    img = torch.empty((1, plan.n_x, plan.n_z), dtype=torch.complex64, device=dev)
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        plan.execute(rf, out=img, stream=stream)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for a, b in evs:
+        flush.zero_()
+        a.record(stream)
+        plan.execute(rf, out=img, stream=stream)
+        b.record(stream)
+    torch.cuda.synchronize()
+    gpu_fps = steps / (sum(a.elapsed_time(b) for a, b in evs) * 1e-3)
+    host_rf = np.ascontiguousarray(wl.rf[0].T)                                 # [T, E]
+    call = lambda: das.gpu_bf_das_pw_rf(wl.positions_x, wl.positions_z, host_rf, wl.f_s, 0.0, wl.array.width,
+                                       wl.array.pitch, wl.c, list(wl.f_bounds), 0, win, fn, None, local)
+    for _ in range(2):
+        call()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        call()
+    e2e_fps = steps / (time.perf_counter() - t0)
+    acc = accuracy_of(wl, win, fn, img[0].cpu().numpy())
+    variant = plan.info()["kernel_variant"]
+    plan.close()
+    cpu_fps, cpu_s, th = cpu_whole_frame(wl, win, fn)
+    return {"workload": config_of(wl, "fused")["workload"], "gpu_value": gpu_fps, "gpu_e2e": e2e_fps,
+            "cpu_value": cpu_fps, "cpu_seconds_per_frame": cpu_s, "cpu_cores": th, "unit": UNIT,
+            "ratio_device": gpu_fps / cpu_fps, "ratio_e2e": e2e_fps / cpu_fps, "kernel_variant": variant,
+            "accuracy": acc,
+            "note": "both arms time complete frames: the GPU over %d steps, the CPU (das_pw.m semantics in C, "
+                    "all host threads) over one frame" % steps}
 
 
 # ---------------------------------------------------------------------------
@@ -413,10 +558,10 @@ def run_saft(args):
            "gterms_per_s": info["terms"] / (np.mean(step_ms) * 1e-3) / 1e9,
            "stage_ms": {"band_dft": float(np.mean([a.elapsed_time(b) for a, b, c in evs])), "beamform": bf_ms},
            "roofline": roof, "clocks": clk,
-           # per step: the symmetrisation kernel (when it applies) and the beamformer; the band
-           # DFT is one cuBLAS SGEMM (a library launch)
-           "gpu_launches": args.steps * (2 if args.kernel == "fused" else 1),
-           "library_launches": {"cublasSgemm (band DFT)": args.steps}}
+           # per step: the band DFT (operand split + tcgen05 GEMM), the symmetrisation kernel
+           # (when it applies) and the beamformer; no library kernels
+           "gpu_launches": args.steps * (4 if args.kernel == "fused" else 3),
+           "library_launches": {}}
     print(json.dumps(out))
     plan.close()
 
@@ -490,9 +635,9 @@ def run_batch(args):
                           "in_batch_completion_p99": float(np.percentile(done, 99)),
                           "sum_of_standalone": float(np.sum(solo))},
            "clocks": clk,
-           # per frame: the band DFT, then per beamform launch the kernel (+ scale and fragment
-           # kernels for the tensor-core variant)
-           "gpu_launches": args.steps * sum(1 + (1 if p.n_out == 1 else p.n_angles) * (3 if v == 9 else 1)
+           # per frame: the band DFT (two kernels), then per beamform launch the kernel (+ scale
+           # and fragment kernels for the tensor-core variant)
+           "gpu_launches": args.steps * sum(2 + (1 if p.n_out == 1 else p.n_angles) * (3 if v == 9 else 1)
                                             for p, v in zip(plans, variants))}
     print(json.dumps(out))
     batch.close()

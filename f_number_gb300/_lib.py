@@ -18,7 +18,8 @@ EXPORTS = (
     "fnum_plan_info_get", "fnum_plan_f_numbers", "fnum_plan_destroy", "fnum_diag_fp32_peak",
     "fnum_das_pw_noalloc", "fnum_bmode", "fnum_plan_autotune", "fnum_batch_create", "fnum_batch_execute",
     "fnum_batch_frame_times", "fnum_batch_destroy", "fnum_pw_plan_set_sound_speed", "fnum_pw_sharpness_grad",
-    "fnum_plan_m_signal", "fnum_plan_set_kernel_variant", "fnum_diag_mma_f16_peak",
+    "fnum_plan_m_signal", "fnum_plan_set_kernel_variant", "fnum_diag_mma_f16_peak", "fnum_host_cache_info",
+    "fnum_plan_spectra", "fnum_pw_adjoint", "fnum_plan_set_spectra", "fnum_das_pw_sharpness_grad",
 )
 
 ABI_VERSION = 3   # FNUM_ABI_VERSION of include/fnum.h
@@ -186,6 +187,16 @@ def lib():
     L.fnum_pw_sharpness_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_int, _dp, _dp, C.c_void_p, C.c_void_p]
     L.fnum_plan_m_signal.restype = C.c_int
     L.fnum_plan_m_signal.argtypes = [C.c_void_p, _dp, _ip]
+    L.fnum_das_pw_sharpness_grad.restype = C.c_int
+    L.fnum_das_pw_sharpness_grad.argtypes = [C.POINTER(PWDesc), _dp, C.c_int, _dp, _dp, _dp, _fp, _fp]
+    L.fnum_pw_adjoint.restype = C.c_int
+    L.fnum_pw_adjoint.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, _dp, C.c_void_p]
+    L.fnum_plan_set_spectra.restype = C.c_int
+    L.fnum_plan_set_spectra.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.fnum_plan_spectra.restype = C.c_int
+    L.fnum_plan_spectra.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.fnum_host_cache_info.restype = C.c_int
+    L.fnum_host_cache_info.argtypes = [C.c_int, C.POINTER(C.c_longlong), _ip]
     L.fnum_bmode.restype = C.c_int
     L.fnum_bmode.argtypes = [C.c_void_p, C.c_longlong, C.c_int, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
     if L.fnum_abi_version() != ABI_VERSION:

@@ -13,7 +13,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libfnum.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["fnum_kernels.cu", "fnum_host.cpp", "fnum_diag.cu", "fnum_noalloc.cu", "fnum_post.cu"]
+SOURCES = ["fnum_kernels.cu", "fnum_host.cpp", "fnum_diag.cu", "fnum_noalloc.cu", "fnum_post.cu", "fnum_dft_tc.cu"]
 
 
 def nvcc() -> str:
@@ -53,7 +53,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         tmp_lib = os.path.join(tmp, "libfnum.so")
         cuda_lib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(cc))), "lib64")
         run([cc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp_lib] + objs +
-            ["-lcublas", "-Xlinker", "-rpath", "-Xlinker", cuda_lib])
+            ["-Xlinker", "-rpath", "-Xlinker", cuda_lib])
         shutil.move(tmp_lib, LIB)
     return LIB
 

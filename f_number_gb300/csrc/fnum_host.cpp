@@ -4,8 +4,9 @@
 // the host-buffer entry points that stand in for the MEX calls.
 #include "../../include/fnum.h"
 #include "fnum_internal.h"
+#include "fnum_host_tables.h"
 
-#include <cublas_v2.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <float.h>
 #include <math.h>
@@ -18,8 +19,9 @@
 #include <vector>
 
 using fnum::dfl;
+using namespace fnum;
 
-namespace {
+namespace fnum {
 
 // ---------------------------------------------------------------------------
 // status
@@ -282,11 +284,6 @@ bool finite_vec(const double* v, int n) {
 // ---------------------------------------------------------------------------
 // band (+cuda/gpu_bf_das_pw_rf.cu:494-556)
 // ---------------------------------------------------------------------------
-struct Band {
-  int N, k_lb, k_ub, K;
-  double coef, add, M;
-};
-
 int compute_band(const double* pz, int nz, int nt, int ne, double fs, double width, double pitch, double c,
                  const double* fb, double t0, Band* b) {
   (void)width;
@@ -424,7 +421,7 @@ void g_table(const std::vector<double>& F, std::vector<dfl>& g) {
     g[i] = ((float)F[i] > FLT_EPSILON) ? to_df(1.0 / (2.0 * F[i])) : make_float2(-1.0f, 0.0f);
 }
 
-}  // namespace
+}  // namespace fnum
 
 // ---------------------------------------------------------------------------
 // plans
@@ -451,20 +448,18 @@ struct fnum_plan {
   double fs = 0.0, pitch = 0.0, width = 0.0, t0 = 0.0, c = 0.0;
   // sharpness-loss gradients (fnum_pw_sharpness_grad), allocated on first use
   float2* adj_img = nullptr;
+  float2* adj_G = nullptr;     // cotangent dL/dI* of the sharpness loss
   float* adj_invw = nullptr;
   float2* adj_H = nullptr;
   float2* adj_gX = nullptr;
   double* adj_sums = nullptr;
   double* adj_acc = nullptr;   // FP64 sums of the voxel slices, 4 per spectrum entry
   bool adj_invw_ready = false;
-  // band DFT as a GEMM: cuBLAS handle, twiddle matrix [nt][2K], PW reorder buffer
-  cublasHandle_t blas = nullptr;
-  float* dftW = nullptr;
-  float2* dftC = nullptr;
+  // band DFT on the tensor cores: fp16 hi/lo operand planes, per-line scales, TMA maps
+  fnum::DftTc dft{};
   // device buffers of the host-buffer entry points (fnum_das_pw / fnum_das_sa), kept for the
   // plan's life so that a cached plan runs without allocating
   double* h_rf = nullptr;
-  float* h_rf32 = nullptr;
   float2* h_img = nullptr;
   float* h_planes = nullptr;   // real plane, then imaginary plane
   float* h_w = nullptr;
@@ -492,19 +487,11 @@ struct fnum_plan {
     return FNUM_OK;
   }
   ~fnum_plan() {
-    if (blas) cublasDestroy(blas);
     for (void* p : allocs) cudaFree(p);
   }
 };
 
-namespace {
-
-// shared geometry tables of both plan kinds
-struct GeomTables {
-  std::vector<dfl> col_u, col_p, col_m, row_u2, row_p, el_u, el_m, el_lb, el_ub;
-  std::vector<int> col_emid;
-  std::vector<float> px_f, pz_f, ctr_f, lb_f, ub_f;
-};
+namespace fnum {
 
 void build_geometry(const double* px, int nx, const double* pz, int nz, int ne, double width, double pitch,
                     double Ku, double M, GeomTables& g) {
@@ -545,6 +532,18 @@ void build_geometry(const double* px, int nx, const double* pz, int nz, int ne, 
     g.ctr_f[e] = (float)(pitch * (e - M));
     g.lb_f[e] = (float)(g.ctr_f[e] - width / 2);
     g.ub_f[e] = (float)(g.ctr_f[e] + width / 2);
+  }
+}
+
+void build_tx_tables(const double* px, int nx, const double* pz, int nz, const double* angles, int na, double Ku,
+                     double M, double pitch, double t0, int N, std::vector<dfl>& ax, std::vector<dfl>& az) {
+  ax.resize((size_t)na * nx);
+  az.resize((size_t)na * nz);
+  for (int a = 0; a < na; ++a) {
+    const double ex = -sin(angles[a]), ez = cos(angles[a]);
+    const double xref = (ex >= 0) ? -M * pitch : M * pitch;  // gpu_bf_das_pw_rf.cu:519
+    for (int i = 0; i < nx; ++i) ax[(size_t)a * nx + i] = to_df(Ku * ex * (px[i] - xref) + t0 / N);
+    for (int j = 0; j < nz; ++j) az[(size_t)a * nz + j] = to_df(Ku * ez * pz[j]);
   }
 }
 
@@ -600,27 +599,18 @@ int check_sa(const fnum_sa_desc* d) {
   return check_device(d->device);
 }
 
-// Band DFT of float RF as one SGEMM (FP32 arithmetic, CUBLAS_PEDANTIC_MATH): the
-// twiddle matrix is built once from the plan's FP64 twiddle table.  Without a cuBLAS
-// handle the plan keeps the band-DFT kernel.
-int setup_gemm_dft(fnum_plan* P, int k_lb, int K, size_t pw_signals) {
-  if (cublasCreate(&P->blas) != CUBLAS_STATUS_SUCCESS) {
-    P->blas = nullptr;
-    return FNUM_OK;
-  }
+// Band DFT on the tensor cores (fnum_dft_tc.cu): the operand planes for nsig RF
+// lines and the twiddle planes, built once from the plan's FP64 twiddle table.
+int setup_tc_dft(fnum_plan* P, int nsig, int k_lb, int K) {
+  const size_t Kp = (size_t)(P->nt + 63) / 64 * 64, Np = (size_t)(2 * K + 127) / 128 * 128;
+  __half_raw* a = nullptr;
+  __half_raw* b = nullptr;
+  float* sc = nullptr;
   int s;
-  void* ws = nullptr;
-  const size_t ws_bytes = 4u << 20;   // fixed workspace: no allocation inside a captured graph
-  if ((s = P->alloc((char**)&ws, ws_bytes))) return s;
-  if (cublasSetWorkspace(P->blas, ws, ws_bytes) != CUBLAS_STATUS_SUCCESS ||
-      cublasSetMathMode(P->blas, CUBLAS_PEDANTIC_MATH) != CUBLAS_STATUS_SUCCESS) {
-    cublasDestroy(P->blas);
-    P->blas = nullptr;
-    return FNUM_OK;
-  }
-  if ((s = P->alloc(&P->dftW, (size_t)P->nt * 2 * K))) return s;
-  if (pw_signals && (s = P->alloc(&P->dftC, pw_signals * K))) return s;
-  cudaError_t e = fnum::launch_dft_matrix(P->tw, P->band.N, P->nt, k_lb, K, P->dftW, 0);
+  if ((s = P->alloc(&a, 2 * (size_t)nsig * Kp)) || (s = P->alloc(&b, 2 * Np * Kp)) || (s = P->alloc(&sc, nsig)))
+    return s;
+  P->info.scratch_bytes += (long long)fnum::dft_tc_bytes(nsig, P->nt, K);
+  cudaError_t e = fnum::dft_tc_setup(P->dft, nsig, P->nt, P->band.N, k_lb, K, P->tw, a, b, sc, 0);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   return e == cudaSuccess ? FNUM_OK : cuda_status(e);
 }
@@ -666,13 +656,13 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
   D.scale = (float)(2.0 / b.N);
   D.x_na = na;
   D.x_a0 = 0;
-  std::vector<dfl> ax((size_t)na * nx), az((size_t)na * nz), gg;
+  std::vector<dfl> ax, az, gg;
+  build_tx_tables(d->positions_x, nx, d->positions_z, nz, angles, na, Ku, b.M, d->element_pitch, d->index_t0, b.N, ax,
+                  az);
   std::vector<float4> txf(na);
   for (int a = 0; a < na; ++a) {
     const double ex = -sin(angles[a]), ez = cos(angles[a]);
     const double xref = (ex >= 0) ? -b.M * d->element_pitch : b.M * d->element_pitch;  // gpu_bf_das_pw_rf.cu:519
-    for (int i = 0; i < nx; ++i) ax[(size_t)a * nx + i] = to_df(Ku * ex * (d->positions_x[i] - xref) + d->index_t0 / b.N);
-    for (int j = 0; j < nz; ++j) az[(size_t)a * nz + j] = to_df(Ku * ez * d->positions_z[j]);
     txf[a] = make_float4((float)ex, (float)ez, (float)xref, 0.0f);
   }
   g_table(P->F, gg);
@@ -764,7 +754,7 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
       goto fail;
     }
   }
-  if ((s = setup_gemm_dft(P, D.k_lb, D.K, (size_t)na * ne))) goto fail;
+  if ((s = setup_tc_dft(P, na * ne, D.k_lb, D.K))) goto fail;
   P->n_out = (flags & FNUM_FLAG_COMPOUND) ? 1 : na;
   P->hx.assign(d->positions_x, d->positions_x + nx);
   P->hz.assign(d->positions_z, d->positions_z + nz);
@@ -894,7 +884,7 @@ int make_sa_plan(const fnum_sa_desc* d, int flags, fnum_plan** out) {
       goto fail;
     }
   }
-  if ((s = setup_gemm_dft(P, D.k_lb, D.K, 0))) goto fail;
+  if ((s = setup_tc_dft(P, ne * ne, D.k_lb, D.K))) goto fail;
   P->n_out = 1;
   P->info.N_dft = b.N; P->info.k_lb = bk.k_lb; P->info.k_ub = bk.k_ub; P->info.n_bins = bk.K;
   P->info.n_x = nx; P->info.n_z = nz; P->info.n_elements = ne; P->info.n_angles = 1; P->info.n_samples = d->n_samples;
@@ -908,31 +898,22 @@ fail:
   return s;
 }
 
+// the band DFT of d_rf into the plan's spectra; counters[5] collects its error bits
 int plan_dft(fnum_plan* P, const void* rf, int is_double, cudaStream_t st) {
-  if (P->blas && !is_double) {
-    const bool pw = P->kind == 0;
-    const int K = pw ? P->pw.K : P->sa.K;
-    const int nsig = pw ? P->pw.na * P->pw.ne : P->sa.ne * P->sa.ne;
-    float2* C = pw ? P->dftC : P->X;
-    const float one = 1.0f, zero = 0.0f;
-    // column-major: C^T [2K x nsig] = W^T [2K x nt] . RF^T [nt x nsig]
-    if (cublasSetStream(P->blas, st) != CUBLAS_STATUS_SUCCESS ||
-        cublasSgemm(P->blas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * K, nsig, P->nt, &one, P->dftW, 2 * K, (const float*)rf,
-                    P->nt, &zero, (float*)C, 2 * K) != CUBLAS_STATUS_SUCCESS)
-      return FNUM_ERR_CUDA;
-    if (pw) return cuda_status(fnum::launch_dft_scatter_pw(C, P->pw.na, P->pw.ne, K, P->X, st));
-    return FNUM_OK;
-  }
+  FNUM_CUDA(cudaMemsetAsync(P->counters + 5, 0, sizeof(unsigned long long), st));
   if (P->kind == 0) {
+    // PW: signal s = a ne + e  ->  X[e][k][a]
     const fnum::PWDev& D = P->pw;
-    return cuda_status(fnum::launch_dft_pw(rf, is_double, D.na, D.ne, P->nt, P->tw, P->band.N, D.k_lb, D.K, P->X, st));
+    return cuda_status(fnum::dft_tc_run(P->dft, rf, is_double, P->X, D.ne, 1, (long long)D.K * D.na, D.na,
+                                        P->counters + 5, st));
   }
+  // SA: signal s = tx ne + rx  ->  X[s][k]
   const fnum::SADev& D = P->sa;
-  return cuda_status(fnum::launch_dft_sa(rf, is_double, D.ne * D.ne, P->nt, P->tw, P->band.N, D.k_lb, D.K, P->X, st));
+  return cuda_status(fnum::dft_tc_run(P->dft, rf, is_double, P->X, D.ne * D.ne, 0, D.K, 1, P->counters + 5, st));
 }
 
 int plan_beamform(fnum_plan* P, void* image, float* w, float* w2, cudaStream_t st) {
-  FNUM_CUDA(cudaMemsetAsync(P->counters, 0, 8 * sizeof(unsigned long long), st));
+  FNUM_CUDA(cudaMemsetAsync(P->counters, 0, 5 * sizeof(unsigned long long), st));   // [5] is the DFT's
   const bool plain = (P->flags & FNUM_FLAG_PLAIN_KERNEL) != 0;
   if (P->kind == 1) {
     cudaError_t e = plain ? fnum::launch_sa_plain(P->sa, (float2*)image, w, w2, st)
@@ -961,30 +942,33 @@ int plan_beamform(fnum_plan* P, void* image, float* w, float* w2, cudaStream_t s
   return FNUM_OK;
 }
 
-// host-buffer execution shared by fnum_das_pw / fnum_das_sa
-int run_host(fnum_plan* P, const double* rf, size_t rf_count, float* re, float* im, float* w, float* w2) {
+// device buffers of the host-buffer entry points, allocated once per plan
+int host_buffers(fnum_plan* P, size_t rf_count) {
   const size_t nvox = (size_t)P->info.n_x * P->info.n_z;
   const size_t nimg = nvox * P->n_out;
   int s = FNUM_OK;
   if (!P->h_rf) {
-    if ((s = P->alloc(&P->h_rf, rf_count)) || (P->blas && (s = P->alloc(&P->h_rf32, rf_count))) ||
+    if ((s = P->alloc(&P->h_rf, rf_count)) ||
         (s = P->alloc(&P->h_img, nimg)) || (s = P->alloc(&P->h_planes, 2 * nimg)) ||
         (s = P->alloc(&P->h_w, nvox)) || (s = P->alloc(&P->h_w2, nvox)))
       return s;
     P->h_rf_count = rf_count;
   }
-  if (rf_count != P->h_rf_count) return FNUM_ERR_ARGUMENT;
+  return rf_count == P->h_rf_count ? FNUM_OK : FNUM_ERR_ARGUMENT;
+}
+
+// host-buffer execution shared by fnum_das_pw / fnum_das_sa
+int run_host(fnum_plan* P, const double* rf, size_t rf_count, float* re, float* im, float* w, float* w2) {
+  const size_t nvox = (size_t)P->info.n_x * P->info.n_z;
+  const size_t nimg = nvox * P->n_out;
+  int s = host_buffers(P, rf_count);
+  if (s) return s;
   float* d_w = w ? P->h_w : nullptr;
   float* d_w2 = w2 ? P->h_w2 : nullptr;
   cudaError_t e = cudaMemcpy(P->h_rf, rf, rf_count * sizeof(double), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_status(e);
-  if (P->blas) {
-    // float RF for the GEMM band DFT
-    if ((e = fnum::launch_to_float(P->h_rf, P->h_rf32, rf_count, 0)) != cudaSuccess) return cuda_status(e);
-    if ((s = plan_dft(P, P->h_rf32, 0, 0))) return s;
-  } else if ((s = plan_dft(P, P->h_rf, 1, 0))) {
-    return s;
-  }
+  // the band DFT rounds double RF to float first, as the reference does
+  if ((s = plan_dft(P, P->h_rf, 1, 0))) return s;
   if ((s = plan_beamform(P, P->h_img, d_w, d_w2, 0))) return s;
   if ((e = fnum::launch_split_complex(P->h_img, nimg, P->h_planes, P->h_planes + nimg, 0)) != cudaSuccess)
     return cuda_status(e);
@@ -995,25 +979,103 @@ int run_host(fnum_plan* P, const double* rf, size_t rf_count, float* re, float* 
   if (e != cudaSuccess) return cuda_status(e);
   unsigned long long c[8];
   if ((e = cudaMemcpy(c, P->counters, sizeof(c), cudaMemcpyDeviceToHost)) != cudaSuccess) return cuda_status(e);
-  if (c[2] & fnum::ERR_SEG_OVERFLOW) return FNUM_ERR_INTERNAL;
+  if ((c[2] & fnum::ERR_SEG_OVERFLOW) || (c[5] & fnum::ERR_DFT_TIMEOUT)) return FNUM_ERR_INTERNAL;
   return FNUM_OK;
 }
 
-// one cached plan per gateway: repeated calls with the same arguments reuse
-// the device tables (the reference allocates and frees everything per call)
+// Plans of the host-buffer gateways, kept across calls: repeated calls with the
+// same arguments reuse the device tables and buffers (the reference allocates
+// and frees everything per call).  The key holds the argument VALUES -- every
+// scalar, position, bound, F value and angle that shapes a plan -- never the
+// addresses of the caller's arrays, so equal geometry in fresh arrays (MATLAB
+// temporaries) finds its plan.  A small least-recently-used list per gateway
+// lets a caller alternate between a few geometries without rebuilding.
+constexpr size_t kPlanCacheEntries = 4;
+
 struct PlanCache {
   std::mutex mu;
-  std::vector<unsigned char> key;
-  fnum_plan* plan = nullptr;
+  std::vector<std::pair<std::vector<unsigned char>, fnum_plan*>> lru;   // most recent last
+  long long created = 0;
 };
 PlanCache g_pw_cache, g_sa_cache;
 
-void key_add(std::vector<unsigned char>& k, const void* p, size_t n) {
-  const unsigned char* c = (const unsigned char*)p;
-  k.insert(k.end(), c, c + n);
+struct KeyWriter {
+  std::vector<unsigned char> k;
+  template <typename T>
+  void put(T v) {
+    const unsigned char* c = (const unsigned char*)&v;
+    k.insert(k.end(), c, c + sizeof(T));
+  }
+  void put_array(const double* p, int n) {
+    put(n);
+    put((int)(p != nullptr));
+    if (p && n > 0) {
+      const unsigned char* c = (const unsigned char*)p;
+      k.insert(k.end(), c, c + sizeof(double) * (size_t)n);
+    }
+  }
+  void put_window(const fnum_window& w) {
+    put(w.id);
+    put(w.parameter);
+  }
+  void put_f_number(const fnum_f_number& f) {
+    put(f.kind);
+    put(f.obliquity);
+    for (double v : f.p) put(v);
+  }
+};
+
+// key of a plane-wave plan: the values of every input that shapes it
+std::vector<unsigned char> pw_key(const fnum_pw_desc* desc, const double* steering_angles, int n_angles, int flags) {
+  KeyWriter kw;
+  kw.put_array(desc->positions_x, desc->n_x);
+  kw.put_array(desc->positions_z, desc->n_z);
+  kw.put(desc->n_samples);
+  kw.put(desc->n_elements);
+  kw.put(desc->f_s);
+  kw.put(desc->element_width);
+  kw.put(desc->element_pitch);
+  kw.put(desc->c_0);
+  kw.put_array(desc->f_bounds, 2);
+  kw.put(desc->index_t0);
+  kw.put_window(desc->window);
+  kw.put_f_number(desc->f_number);
+  kw.put_array(desc->f_number_values, desc->f_number_values ? desc->n_f_number_values : 0);
+  kw.put(desc->normalization);
+  kw.put(desc->device);
+  kw.put_window(desc->normalization_window);
+  kw.put_array(steering_angles, n_angles);
+  kw.put(flags);
+  return kw.k;
 }
 
-}  // namespace
+// the cached plan for `key`, or a new one from `make` (which may fail); the
+// least recently used plan is destroyed when the list is full
+template <typename Make>
+int cached_plan(PlanCache& C, const std::vector<unsigned char>& key, Make make, fnum_plan** out) {
+  for (size_t i = 0; i < C.lru.size(); ++i) {
+    if (C.lru[i].first == key) {
+      auto hit = C.lru[i];
+      C.lru.erase(C.lru.begin() + (long)i);
+      C.lru.push_back(hit);
+      *out = hit.second;
+      return FNUM_OK;
+    }
+  }
+  fnum_plan* P = nullptr;
+  const int s = make(&P);
+  if (s) return s;
+  ++C.created;
+  if (C.lru.size() >= kPlanCacheEntries) {
+    fnum_plan_destroy(C.lru.front().second);
+    C.lru.erase(C.lru.begin());
+  }
+  C.lru.emplace_back(key, P);
+  *out = P;
+  return FNUM_OK;
+}
+
+}  // namespace fnum
 
 // ---------------------------------------------------------------------------
 // exported C ABI
@@ -1106,6 +1168,15 @@ int fnum_plan_execute(fnum_plan* plan, const void* d_rf, int rf_is_double, void*
   return plan_beamform(plan, d_image, d_weights, d_weights_rx, (cudaStream_t)stream);
 }
 
+int fnum_plan_spectra(const fnum_plan* plan, void* d_spectra, void* stream) {
+  if (!plan || !d_spectra) return FNUM_ERR_ARGUMENT;
+  FNUM_CUDA(cudaSetDevice(plan->device));
+  const size_t n = plan->kind == 0 ? (size_t)plan->pw.ne * plan->pw.K * plan->pw.na
+                                   : (size_t)plan->sa.ne * plan->sa.ne * plan->sa.K;
+  FNUM_CUDA(cudaMemcpyAsync(d_spectra, plan->X, n * sizeof(float2), cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+  return FNUM_OK;
+}
+
 int fnum_plan_info_get(const fnum_plan* plan, fnum_plan_info* info) {
   if (!plan || !info) return FNUM_ERR_ARGUMENT;
   *info = plan->info;
@@ -1121,7 +1192,7 @@ int fnum_plan_info_get(const fnum_plan* plan, fnum_plan_info* info) {
   info->executed_terms = (long long)c[4];
   info->kernel_variant = plan->kind == 0 ? fnum::pw_variant_of(plan->pw) : 0;
   info->grid = plan->grid;
-  if (c[2] & fnum::ERR_SEG_OVERFLOW) return FNUM_ERR_INTERNAL;
+  if ((c[2] & fnum::ERR_SEG_OVERFLOW) || (c[5] & fnum::ERR_DFT_TIMEOUT)) return FNUM_ERR_INTERNAL;
   return FNUM_OK;
 }
 
@@ -1145,28 +1216,56 @@ int fnum_das_pw(const fnum_pw_desc* desc, const double* steering_angles, int n_a
   if (!desc || !data_rf || !image_re || !image_im) return FNUM_ERR_ARGUMENT;
   int s = check_pw(desc, steering_angles, n_angles);
   if (s) return s;
-  // cache key: every input that shapes the plan
-  std::vector<unsigned char> key;
-  key_add(key, desc, sizeof(*desc));
-  key_add(key, desc->positions_x, sizeof(double) * desc->n_x);
-  key_add(key, desc->positions_z, sizeof(double) * desc->n_z);
-  if (desc->f_bounds) key_add(key, desc->f_bounds, 2 * sizeof(double));
-  if (desc->f_number_values) key_add(key, desc->f_number_values, sizeof(double) * desc->n_f_number_values);
-  key_add(key, steering_angles, sizeof(double) * n_angles);
-  key_add(key, &flags, sizeof(flags));
+  // cache key: the values of every input that shapes the plan
+  const std::vector<unsigned char> key = pw_key(desc, steering_angles, n_angles, flags);
   std::lock_guard<std::mutex> lock(g_pw_cache.mu);
   FNUM_CUDA(cudaSetDevice(desc->device));
-  if (!g_pw_cache.plan || g_pw_cache.key != key) {
-    fnum_plan_destroy(g_pw_cache.plan);
-    g_pw_cache.plan = nullptr;
-    g_pw_cache.key.clear();
-    fnum_plan* P = nullptr;
-    if ((s = make_pw_plan(desc, steering_angles, n_angles, flags, &P))) return s;
-    g_pw_cache.plan = P;
-    g_pw_cache.key = key;
-  }
+  fnum_plan* P = nullptr;
+  if ((s = cached_plan(g_pw_cache, key,
+                       [&](fnum_plan** p) { return make_pw_plan(desc, steering_angles, n_angles, flags, p); }, &P)))
+    return s;
   const size_t rf_count = (size_t)n_angles * desc->n_elements * desc->n_samples;
-  return run_host(g_pw_cache.plan, data_rf, rf_count, image_re, image_im, weights, nullptr);
+  return run_host(P, data_rf, rf_count, image_re, image_im, weights, nullptr);
+}
+
+int fnum_das_pw_sharpness_grad(const fnum_pw_desc* desc, const double* steering_angles, int n_angles,
+                               const double* data_rf, double* loss, double* dloss_dc, float* grad_re,
+                               float* grad_im) {
+  if (!desc || !data_rf) return FNUM_ERR_ARGUMENT;
+  int s = check_pw(desc, steering_angles, n_angles);
+  if (s) return s;
+  const std::vector<unsigned char> key = pw_key(desc, steering_angles, n_angles, FNUM_FLAG_COMPOUND);
+  std::lock_guard<std::mutex> lock(g_pw_cache.mu);
+  FNUM_CUDA(cudaSetDevice(desc->device));
+  fnum_plan* P = nullptr;
+  if ((s = cached_plan(g_pw_cache, key,
+                       [&](fnum_plan** p) {
+                         return make_pw_plan(desc, steering_angles, n_angles, FNUM_FLAG_COMPOUND, p);
+                       },
+                       &P)))
+    return s;
+  const size_t rf_count = (size_t)n_angles * desc->n_elements * desc->n_samples;
+  if ((s = host_buffers(P, rf_count))) return s;
+  FNUM_CUDA(cudaMemcpy(P->h_rf, data_rf, rf_count * sizeof(double), cudaMemcpyHostToDevice));
+  if ((s = fnum_pw_sharpness_grad(P, P->h_rf, 1, loss, dloss_dc, nullptr, nullptr))) return s;
+  if (grad_re || grad_im) {
+    // plan layout [e][k][a] -> [a][e][k] (bins fastest, MATLAB's [N_bins x N_el x N_angles])
+    const fnum::PWDev& D = P->pw;
+    std::vector<float2> g((size_t)D.ne * D.K * D.na);
+    FNUM_CUDA(cudaMemcpy(g.data(), P->adj_gX, g.size() * sizeof(float2), cudaMemcpyDeviceToHost));
+    for (int a = 0; a < D.na; ++a)
+      for (int e = 0; e < D.ne; ++e)
+        for (int k = 0; k < D.K; ++k) {
+          const float2 v = g[((size_t)e * D.K + k) * D.na + a];
+          const size_t o = ((size_t)a * D.ne + e) * D.K + k;
+          if (grad_re) grad_re[o] = v.x;
+          if (grad_im) grad_im[o] = v.y;
+        }
+  }
+  unsigned long long c[8];
+  FNUM_CUDA(cudaMemcpy(c, P->counters, sizeof(c), cudaMemcpyDeviceToHost));
+  if ((c[2] & fnum::ERR_SEG_OVERFLOW) || (c[5] & fnum::ERR_DFT_TIMEOUT)) return FNUM_ERR_INTERNAL;
+  return FNUM_OK;
 }
 
 int fnum_das_sa(const fnum_sa_desc* desc, const double* data_rf, int flags, float* image_re, float* image_im,
@@ -1174,27 +1273,42 @@ int fnum_das_sa(const fnum_sa_desc* desc, const double* data_rf, int flags, floa
   if (!desc || !data_rf || !image_re || !image_im) return FNUM_ERR_ARGUMENT;
   int s = check_sa(desc);
   if (s) return s;
-  std::vector<unsigned char> key;
-  key_add(key, desc, sizeof(*desc));
-  key_add(key, desc->positions_x, sizeof(double) * desc->n_x);
-  key_add(key, desc->positions_z, sizeof(double) * desc->n_z);
-  if (desc->f_bounds) key_add(key, desc->f_bounds, 2 * sizeof(double));
-  if (desc->f_number_tx_values) key_add(key, desc->f_number_tx_values, sizeof(double) * desc->n_f_number_values);
-  if (desc->f_number_rx_values) key_add(key, desc->f_number_rx_values, sizeof(double) * desc->n_f_number_values);
-  key_add(key, &flags, sizeof(flags));
+  KeyWriter kw;
+  kw.put_array(desc->positions_x, desc->n_x);
+  kw.put_array(desc->positions_z, desc->n_z);
+  kw.put(desc->n_samples);
+  kw.put(desc->n_elements);
+  kw.put(desc->f_s);
+  kw.put(desc->element_width);
+  kw.put(desc->element_pitch);
+  kw.put(desc->c_0);
+  kw.put_array(desc->f_bounds, 2);
+  kw.put(desc->index_t0);
+  kw.put_window(desc->window_tx);
+  kw.put_window(desc->window_rx);
+  kw.put_f_number(desc->f_number_tx);
+  kw.put_f_number(desc->f_number_rx);
+  const int nfv = desc->n_f_number_values;
+  kw.put_array(desc->f_number_tx_values, desc->f_number_tx_values ? nfv : 0);
+  kw.put_array(desc->f_number_rx_values, desc->f_number_rx_values ? nfv : 0);
+  kw.put(desc->normalization_tx);
+  kw.put(desc->normalization_rx);
+  kw.put(desc->device);
+  kw.put(flags);
   std::lock_guard<std::mutex> lock(g_sa_cache.mu);
   FNUM_CUDA(cudaSetDevice(desc->device));
-  if (!g_sa_cache.plan || g_sa_cache.key != key) {
-    fnum_plan_destroy(g_sa_cache.plan);
-    g_sa_cache.plan = nullptr;
-    g_sa_cache.key.clear();
-    fnum_plan* P = nullptr;
-    if ((s = make_sa_plan(desc, flags, &P))) return s;
-    g_sa_cache.plan = P;
-    g_sa_cache.key = key;
-  }
+  fnum_plan* P = nullptr;
+  if ((s = cached_plan(g_sa_cache, kw.k, [&](fnum_plan** p) { return make_sa_plan(desc, flags, p); }, &P))) return s;
   const size_t rf_count = (size_t)desc->n_elements * desc->n_elements * desc->n_samples;
-  return run_host(g_sa_cache.plan, data_rf, rf_count, image_re, image_im, weights_tx, weights_rx);
+  return run_host(P, data_rf, rf_count, image_re, image_im, weights_tx, weights_rx);
+}
+
+int fnum_host_cache_info(int saft, long long* plans_created, int* plans_cached) {
+  PlanCache& C = saft ? g_sa_cache : g_pw_cache;
+  std::lock_guard<std::mutex> lock(C.mu);
+  if (plans_created) *plans_created = C.created;
+  if (plans_cached) *plans_cached = (int)C.lru.size();
+  return FNUM_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -1414,14 +1528,9 @@ int fnum_pw_plan_set_sound_speed(fnum_plan* plan, double c_0) {
   const double Ku = plan->fs / ((double)b.N * c_0);
   GeomTables g;
   build_geometry(plan->hx.data(), D.nx, plan->hz.data(), D.nz, D.ne, plan->width, plan->pitch, Ku, b.M, g);
-  const int na = D.na;
-  std::vector<dfl> ax((size_t)na * D.nx), az((size_t)na * D.nz);
-  for (int a = 0; a < na; ++a) {
-    const double ex = -sin(plan->hang[a]), ez = cos(plan->hang[a]);
-    const double xref = (ex >= 0) ? -b.M * plan->pitch : b.M * plan->pitch;
-    for (int i = 0; i < D.nx; ++i) ax[(size_t)a * D.nx + i] = to_df(Ku * ex * (plan->hx[i] - xref) + plan->t0 / b.N);
-    for (int j = 0; j < D.nz; ++j) az[(size_t)a * D.nz + j] = to_df(Ku * ez * plan->hz[j]);
-  }
+  std::vector<dfl> ax, az;
+  build_tx_tables(plan->hx.data(), D.nx, plan->hz.data(), D.nz, plan->hang.data(), D.na, Ku, b.M, plan->pitch,
+                  plan->t0, b.N, ax, az);
   FNUM_CUDA(cudaMemcpy((void*)D.col_u, g.col_u.data(), g.col_u.size() * sizeof(dfl), cudaMemcpyHostToDevice));
   FNUM_CUDA(cudaMemcpy((void*)D.row_u2, g.row_u2.data(), g.row_u2.size() * sizeof(dfl), cudaMemcpyHostToDevice));
   FNUM_CUDA(cudaMemcpy((void*)D.el_u, g.el_u.data(), g.el_u.size() * sizeof(dfl), cudaMemcpyHostToDevice));
@@ -1432,25 +1541,78 @@ int fnum_pw_plan_set_sound_speed(fnum_plan* plan, double c_0) {
   return FNUM_OK;
 }
 
-int fnum_pw_sharpness_grad(fnum_plan* plan, const void* d_rf, int rf_is_double, double* loss, double* dloss_dc,
-                           void* d_grad_spectra, void* stream) {
-  if (!plan || !d_rf || plan->kind != 0 || plan->n_out != 1) return FNUM_ERR_ARGUMENT;
-  FNUM_CUDA(cudaSetDevice(plan->device));
-  cudaStream_t st = (cudaStream_t)stream;
-  fnum::PWDev& D = plan->pw;
+namespace fnum {
+
+// gradient buffers of a compounded plane-wave plan, allocated on first use; the 1/W
+// table of the frozen apertures is built once
+int adjoint_buffers(fnum_plan* plan, cudaStream_t st) {
+  const fnum::PWDev& D = plan->pw;
   const long long nvox = (long long)D.nx * D.nz;
   const size_t nspec = (size_t)D.ne * D.K * D.na;
   int s = FNUM_OK;
   if (!plan->adj_img) {
-    if ((s = plan->alloc(&plan->adj_img, (size_t)nvox)) || (s = plan->alloc(&plan->adj_invw, (size_t)nvox * D.K)) ||
-        (s = plan->alloc(&plan->adj_H, nspec)) || (s = plan->alloc(&plan->adj_gX, nspec)) ||
-        (s = plan->alloc(&plan->adj_sums, 4)) || (s = plan->alloc(&plan->adj_acc, 4 * nspec)))
+    if ((s = plan->alloc(&plan->adj_img, (size_t)nvox)) || (s = plan->alloc(&plan->adj_G, (size_t)nvox)) ||
+        (s = plan->alloc(&plan->adj_invw, (size_t)nvox * D.K)) || (s = plan->alloc(&plan->adj_H, nspec)) ||
+        (s = plan->alloc(&plan->adj_gX, nspec)) || (s = plan->alloc(&plan->adj_sums, 4)) ||
+        (s = plan->alloc(&plan->adj_acc, 4 * nspec)))
       return s;
   }
   if (!plan->adj_invw_ready) {
     FNUM_CUDA(fnum::launch_pw_invw(D, plan->adj_invw, st));
     plan->adj_invw_ready = true;
   }
+  return FNUM_OK;
+}
+
+// dL/dX* into gX and (if dloss_dc) dL/dc for the cotangent G = dL/dI*, on the plan's spectra
+int adjoint_core(fnum_plan* plan, const float2* G, float2* gX, double* dloss_dc, cudaStream_t st) {
+  fnum::PWDev& D = plan->pw;
+  FNUM_CUDA(fnum::launch_pw_adjoint(D, G, plan->adj_invw, (float)(plan->t0 / plan->band.N), gX, plan->adj_H,
+                                    plan->adj_acc, st));
+  if (dloss_dc) {
+    const double coef = 4.0 * M_PI * (2.0 / plan->band.N) / plan->c;
+    FNUM_CUDA(fnum::launch_pw_dldc(D, plan->adj_H, coef, plan->adj_sums + 2, st));
+    double g = 0.0;
+    FNUM_CUDA(cudaMemcpyAsync(&g, plan->adj_sums + 2, sizeof(double), cudaMemcpyDeviceToHost, st));
+    FNUM_CUDA(cudaStreamSynchronize(st));
+    *dloss_dc = g;
+  } else {
+    FNUM_CUDA(cudaStreamSynchronize(st));
+  }
+  return FNUM_OK;
+}
+
+}  // namespace fnum
+
+int fnum_plan_set_spectra(fnum_plan* plan, const void* d_spectra, void* stream) {
+  if (!plan || !d_spectra) return FNUM_ERR_ARGUMENT;
+  FNUM_CUDA(cudaSetDevice(plan->device));
+  const size_t n = plan->kind == 0 ? (size_t)plan->pw.ne * plan->pw.K * plan->pw.na
+                                   : (size_t)plan->sa.ne * plan->sa.ne * plan->sa.K;
+  FNUM_CUDA(cudaMemcpyAsync(plan->X, d_spectra, n * sizeof(float2), cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+  return FNUM_OK;
+}
+
+int fnum_pw_adjoint(fnum_plan* plan, const void* d_cotangent, void* d_grad_spectra, double* dloss_dc, void* stream) {
+  if (!plan || !d_cotangent || plan->kind != 0 || plan->n_out != 1 || plan->pw.m_sem) return FNUM_ERR_ARGUMENT;
+  FNUM_CUDA(cudaSetDevice(plan->device));
+  cudaStream_t st = (cudaStream_t)stream;
+  int s;
+  if ((s = fnum::adjoint_buffers(plan, st))) return s;
+  float2* gX = d_grad_spectra ? (float2*)d_grad_spectra : plan->adj_gX;
+  return fnum::adjoint_core(plan, (const float2*)d_cotangent, gX, dloss_dc, st);
+}
+
+int fnum_pw_sharpness_grad(fnum_plan* plan, const void* d_rf, int rf_is_double, double* loss, double* dloss_dc,
+                           void* d_grad_spectra, void* stream) {
+  if (!plan || !d_rf || plan->kind != 0 || plan->n_out != 1 || plan->pw.m_sem) return FNUM_ERR_ARGUMENT;
+  FNUM_CUDA(cudaSetDevice(plan->device));
+  cudaStream_t st = (cudaStream_t)stream;
+  fnum::PWDev& D = plan->pw;
+  const long long nvox = (long long)D.nx * D.nz;
+  const size_t nspec = (size_t)D.ne * D.K * D.na;
+  int s = FNUM_OK;
+  if ((s = fnum::adjoint_buffers(plan, st))) return s;
   if ((s = plan_dft(plan, d_rf, rf_is_double, st))) return s;
   if ((s = plan_beamform(plan, plan->adj_img, nullptr, nullptr, st))) return s;
   FNUM_CUDA(fnum::launch_pw_sharp_sums(plan->adj_img, nvox, plan->adj_sums, st));
@@ -1466,15 +1628,9 @@ int fnum_pw_sharpness_grad(fnum_plan* plan, const void* d_rf, int rf_is_double, 
     return FNUM_OK;
   }
   const double gs2 = 1.0 / (S[0] * S[0]), gs4 = S[1] / (S[0] * S[0] * S[0]);
-  FNUM_CUDA(fnum::launch_pw_adjoint(D, plan->adj_img, plan->adj_invw, (float)gs2, (float)gs4,
-                                    (float)(plan->t0 / plan->band.N), gX, plan->adj_H, plan->adj_acc, st));
-  const double coef = 4.0 * M_PI * (2.0 / plan->band.N) / plan->c;
-  FNUM_CUDA(fnum::launch_pw_dldc(D, plan->adj_H, coef, plan->adj_sums + 2, st));
-  double g = 0.0;
-  FNUM_CUDA(cudaMemcpyAsync(&g, plan->adj_sums + 2, sizeof(double), cudaMemcpyDeviceToHost, st));
-  FNUM_CUDA(cudaStreamSynchronize(st));
+  FNUM_CUDA(fnum::launch_pw_sharp_cotangent(plan->adj_img, nvox, (float)gs2, (float)gs4, plan->adj_G, st));
+  if ((s = fnum::adjoint_core(plan, plan->adj_G, gX, dloss_dc, st))) return s;
   if (loss) *loss = -S[1] / (S[0] * S[0]);
-  if (dloss_dc) *dloss_dc = g;
   return FNUM_OK;
 }
 

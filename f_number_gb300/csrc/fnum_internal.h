@@ -1,7 +1,9 @@
 // Internal plan layout shared by the host library (fnum_host.cpp) and the
 // kernels (fnum_kernels.cu).  Not part of the public ABI.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 namespace fnum {
@@ -112,8 +114,30 @@ struct SADev {
   float M_f, pitch_f, coef_f, add_f;
 };
 
-// error bits in counters[2]
+// error bits in counters[2] (beamformers) and counters[5] (band DFT)
 constexpr unsigned long long ERR_SEG_OVERFLOW = 1ull;
+constexpr unsigned long long ERR_DFT_TIMEOUT = 2ull;   // a wait of the tensor-core DFT gave up
+
+// Band DFT on the tensor cores (fnum_dft_tc.cu): RF lines split into fp16 hi/lo
+// planes a [2][nsig][Kp], twiddle planes b [2][Np][Kp], per-line scale; the TMA
+// maps of the four planes are built once per plan.
+struct DftTc {
+  CUtensorMap tm[4];   // A hi, A lo, B hi, B lo (64-byte aligned)
+  void* a;
+  void* b;
+  float* inv_scale;
+  int nsig, nt, N, k_lb, K, Kp, Np;
+};
+// device bytes of a, b and inv_scale for nsig lines of nt samples and K bins
+size_t dft_tc_bytes(int nsig, int nt, int K);
+// binds the buffers (a: 2 nsig Kp halves, b: 2 Np Kp halves, inv_scale: nsig floats),
+// builds the TMA maps and fills b from the twiddle table on stream s
+cudaError_t dft_tc_setup(DftTc& d, int nsig, int nt, int N, int k_lb, int K, const float2* tw, void* a, void* b,
+                         float* inv_scale, cudaStream_t s);
+// rf [nsig][nt] (float or double) -> X[(sig / lo_n) s_hi + (sig % lo_n) s_lo + k' s_k];
+// ERR_DFT_TIMEOUT is or-ed into *err if a wait gave up
+cudaError_t dft_tc_run(const DftTc& d, const void* rf, int is_double, float2* X, int lo_n, long long s_hi,
+                       long long s_lo, long long s_k, unsigned long long* err, cudaStream_t s);
 
 // --- launchers (fnum_kernels.cu) -------------------------------------------
 cudaError_t launch_twiddles(float2* tw, int N, cudaStream_t s);
@@ -122,10 +146,6 @@ cudaError_t launch_dft_pw(const void* rf, int is_double, int na, int ne, int nt,
                           int k_lb, int K, float2* X, cudaStream_t s);
 cudaError_t launch_dft_sa(const void* rf, int is_double, int nsig, int nt, const float2* tw, int N, int k_lb,
                           int K, float2* X, cudaStream_t s);
-// band DFT as a GEMM: twiddle matrix [nt][2K], PW reorder, double -> float
-cudaError_t launch_dft_matrix(const float2* tw, int N, int nt, int k_lb, int K, float* W, cudaStream_t s);
-cudaError_t launch_dft_scatter_pw(const float2* C, int na, int ne, int K, float2* X, cudaStream_t s);
-cudaError_t launch_to_float(const double* in, float* out, size_t n, cudaStream_t s);
 cudaError_t launch_split_complex(const float2* in, size_t n, float* re, float* im, cudaStream_t s);
 int pw_fused_grid(const PWDev& d, int* blocks_per_sm);   // grid of d's variant, all blocks resident
 int pw_fused_max_grid(const PWDev& d);                     // largest of those over the variants
@@ -141,8 +161,12 @@ cudaError_t launch_sa_plain(const SADev& d, float2* image, float* wtx, float* wr
 // sharpness-loss gradients of a compounded plane-wave plan (fnum_pw_sharpness_grad)
 cudaError_t launch_pw_invw(const PWDev& d, float* invw, cudaStream_t s);
 cudaError_t launch_pw_sharp_sums(const float2* img, long long n, double* sums, cudaStream_t s);
-cudaError_t launch_pw_adjoint(const PWDev& d, const float2* img, const float* invw, float gs2, float gs4, float t0N,
-                              float2* gX, float2* H, double* acc, cudaStream_t s);   // acc: 4 doubles per spectrum entry
+// G = dL/dI* of the sharpness loss from the image and its sums (gs2 = 1/S2^2, gs4 = S4/S2^3)
+cudaError_t launch_pw_sharp_cotangent(const float2* img, long long n, float gs2, float gs4, float2* G, cudaStream_t s);
+// adjoint of the compounded beamformer for a cotangent G = dL/dI* [nx][nz]: gX = dL/dX* and
+// H = sum_v G_v b e^{-2 pi i k u} U (for dL/dc); acc: 4 doubles per spectrum entry
+cudaError_t launch_pw_adjoint(const PWDev& d, const float2* cot, const float* invw, float t0N, float2* gX, float2* H,
+                              double* acc, cudaStream_t s);
 cudaError_t launch_pw_dldc(const PWDev& d, const float2* H, double coef, double* out, cudaStream_t s);
 
 }  // namespace fnum

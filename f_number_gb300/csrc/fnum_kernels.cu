@@ -301,38 +301,6 @@ cudaError_t launch_dft_sa(const void* rf, int is_double, int nsig, int nt, const
   return dft_launch(rf, is_double, nsig, nt, tw, N, k_lb, K, X, 1, 0, K, nsig, s);
 }
 
-// The band DFT as a GEMM (cuBLAS SGEMM on the host side): spectra [signal][2K] =
-// RF [signal][nt] . W [nt][2K], W[t][2k'] + j W[t][2k'+1] = e^{-j 2 pi (k_lb + k') t / N}
-// with the index (k t) mod N exact in integers and the twiddles of the FP64 table.
-__global__ void dft_matrix_kernel(const float2* __restrict__ tw, int N, int nt, int k_lb, int K, float* __restrict__ W) {
-  const size_t n = (size_t)nt * K;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const long long t = (long long)(i / K), kk = (long long)(i % K);
-    const float2 w = tw[(t * (k_lb + kk)) % N];
-    W[t * 2 * K + 2 * kk] = w.x;
-    W[t * 2 * K + 2 * kk + 1] = w.y;
-  }
-}
-cudaError_t launch_dft_matrix(const float2* tw, int N, int nt, int k_lb, int K, float* W, cudaStream_t s) {
-  dft_matrix_kernel<<<1216, 256, 0, s>>>(tw, N, nt, k_lb, K, W);
-  return cudaGetLastError();
-}
-
-// PW spectra from the GEMM's [a * ne + e][k] order to the beamformer's [e][k][a]
-__global__ void dft_scatter_pw_kernel(const float2* __restrict__ C, int na, int ne, int K, float2* __restrict__ X) {
-  const size_t n = (size_t)na * ne * K;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const int a = (int)(i % na);
-    const size_t ek = i / na;
-    const int k = (int)(ek % K), e = (int)(ek / K);
-    X[i] = C[((size_t)a * ne + e) * K + k];
-  }
-}
-cudaError_t launch_dft_scatter_pw(const float2* C, int na, int ne, int K, float2* X, cudaStream_t s) {
-  dft_scatter_pw_kernel<<<1216, 256, 0, s>>>(C, na, ne, K, X);
-  return cudaGetLastError();
-}
-
 // complex image -> separate real and imaginary planes (the MEX output layout)
 __global__ void split_complex_kernel(const float2* __restrict__ in, size_t n, float* __restrict__ re,
                                      float* __restrict__ im) {
@@ -344,15 +312,6 @@ __global__ void split_complex_kernel(const float2* __restrict__ in, size_t n, fl
 }
 cudaError_t launch_split_complex(const float2* in, size_t n, float* re, float* im, cudaStream_t s) {
   split_complex_kernel<<<608, 256, 0, s>>>(in, n, re, im);
-  return cudaGetLastError();
-}
-
-__global__ void to_float_kernel(const double* __restrict__ in, float* __restrict__ out, size_t n) {
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    out[i] = (float)in[i];
-}
-cudaError_t launch_to_float(const double* in, float* out, size_t n, cudaStream_t s) {
-  to_float_kernel<<<1216, 256, 0, s>>>(in, out, n);
   return cudaGetLastError();
 }
 
@@ -2473,8 +2432,8 @@ constexpr int ADJ_VB = 128;
 constexpr int ADJ_SLICE = 8192;   // voxels per block: the grid is bins x voxel slices
 template <int WIN>
 __global__ void __launch_bounds__(128, 4)
-pw_adjoint_kernel(const PWDev d, const float2* __restrict__ img, const float* __restrict__ invw, float gs2, float gs4,
-                  float t0N, double* __restrict__ acc) {
+pw_adjoint_kernel(const PWDev d, const float2* __restrict__ cot, const float* __restrict__ invw, float t0N,
+                  double* __restrict__ acc) {
   __shared__ float2 sT[ADJ_VB][ADJ_NA];   // transmit phasor
   __shared__ float sUt[ADJ_VB][ADJ_NA];   // u_tx - t0/N
   __shared__ float2 sG[ADJ_VB];           // G_v / W_{v,k} (0: no contribution)
@@ -2507,9 +2466,8 @@ pw_adjoint_kernel(const PWDev d, const float2* __restrict__ img, const float* __
           int ilb, iub;
           aperture(d.col_p[i], d.row_p[j], g, d.ne, ilb, iub);
           const float iw = invw[(size_t)v * d.K + kk];
-          const float2 I = img[v];
-          const float cg = -2.0f * ((I.x * I.x + I.y * I.y) * gs2 - gs4) * iw;
-          sG[q] = make_float2(cg * I.x, cg * I.y);
+          const float2 G = cot[v];
+          sG[q] = make_float2(G.x * iw, G.y * iw);
           sAp[q][0] = ilb;
           sAp[q][1] = iub;
           sAp[q][2] = d.col_emid[i];
@@ -2630,18 +2588,33 @@ __global__ void __launch_bounds__(256) pw_adjoint_finish_kernel(const double* __
   }
 }
 
-cudaError_t launch_pw_adjoint(const PWDev& d, const float2* img, const float* invw, float gs2, float gs4, float t0N,
-                              float2* gX, float2* H, double* acc, cudaStream_t s) {
+// cotangent of the sharpness loss L = -S4 / S2^2: dL/dI*_v = -2 I_v (|I_v|^2 / S2^2 - S4 / S2^3)
+__global__ void __launch_bounds__(256) pw_sharp_cotangent_kernel(const float2* __restrict__ img, long long n, float gs2,
+                                                                 float gs4, float2* __restrict__ G) {
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+    const float2 I = img[v];
+    const float cg = -2.0f * ((I.x * I.x + I.y * I.y) * gs2 - gs4);
+    G[v] = make_float2(cg * I.x, cg * I.y);
+  }
+}
+
+cudaError_t launch_pw_sharp_cotangent(const float2* img, long long n, float gs2, float gs4, float2* G, cudaStream_t s) {
+  pw_sharp_cotangent_kernel<<<1216, 256, 0, s>>>(img, n, gs2, gs4, G);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pw_adjoint(const PWDev& d, const float2* cot, const float* invw, float t0N, float2* gX, float2* H,
+                              double* acc, cudaStream_t s) {
   const size_t n = (size_t)d.ne * d.K * d.na;
   cudaError_t e = cudaMemsetAsync(acc, 0, 4 * n * sizeof(double), s);
   if (e != cudaSuccess) return e;
   const long long nvox = (long long)d.nx * d.nz;
   const dim3 grid(d.K, (unsigned)((nvox + ADJ_SLICE - 1) / ADJ_SLICE));
   switch (d.window_id) {
-    case 0: pw_adjoint_kernel<0><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, acc); break;
-    case 1: pw_adjoint_kernel<1><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, acc); break;
-    case 2: pw_adjoint_kernel<2><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, acc); break;
-    default: pw_adjoint_kernel<4><<<grid, 128, 0, s>>>(d, img, invw, gs2, gs4, t0N, acc); break;
+    case 0: pw_adjoint_kernel<0><<<grid, 128, 0, s>>>(d, cot, invw, t0N, acc); break;
+    case 1: pw_adjoint_kernel<1><<<grid, 128, 0, s>>>(d, cot, invw, t0N, acc); break;
+    case 2: pw_adjoint_kernel<2><<<grid, 128, 0, s>>>(d, cot, invw, t0N, acc); break;
+    default: pw_adjoint_kernel<4><<<grid, 128, 0, s>>>(d, cot, invw, t0N, acc); break;
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;

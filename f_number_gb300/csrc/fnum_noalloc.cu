@@ -21,11 +21,13 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
 #include "../../include/fnum.h"
 #include "fnum_internal.h"
+#include "fnum_host_tables.h"
 
 namespace {
 
@@ -40,7 +42,10 @@ void* g_scratch_ptr[kMaxDevices] = {nullptr};
 
 // Device address of the scratch array for the current device: taken once per
 // device, with that device current.  In host code the symbol itself is only a
-// host-side stand-in; the kernels must be given this address.
+// host-side stand-in; the kernels must be given this address.  The address is
+// kept for the life of the process, so a host must not reset the device
+// (cudaDeviceReset, MATLAB's reset(gpuDevice)) between calls: a reset reloads
+// the library's device code and may move the array.
 int scratch_address(int device, unsigned char** out) {
   if (device < 0 || device >= kMaxDevices) return FNUM_ERR_INVALID_DEVICE;
   std::lock_guard<std::mutex> lock(g_mu);
@@ -69,112 +74,45 @@ struct Carve {
   }
 };
 
-dfl to_df(double v) {
-  const float hi = (float)v;
-  return make_float2(hi, (float)(v - (double)hi));
-}
-
 }  // namespace
 
 extern "C" int fnum_das_pw_noalloc(const fnum_pw_desc* desc, const double* steering_angles, int n_angles,
                                    const float* d_rf, int flags, void* d_image, float* d_weights, void* stream) {
-  if (!desc || !steering_angles || !d_rf || !d_image || n_angles < 1) return FNUM_ERR_ARGUMENT;
+  if (!desc || !d_rf || !d_image) return FNUM_ERR_ARGUMENT;
   if (flags & ~FNUM_FLAG_COMPOUND) return FNUM_ERR_ARGUMENT;  // fused kernel, reference semantics only
   const cudaStream_t st = (cudaStream_t)stream;
-  int n_dev = 0;
-  if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev < 1) {
-    (void)cudaGetLastError();
-    return FNUM_ERR_NO_DEVICE;
-  }
-  if (desc->device < 0 || desc->device >= n_dev) return FNUM_ERR_INVALID_DEVICE;
+  // the plan path's checks, in the gateway's order and with its identifiers
+  int s = fnum::check_pw(desc, steering_angles, n_angles);
+  if (s != FNUM_OK) return s;
   if (cudaSetDevice(desc->device) != cudaSuccess) {
     (void)cudaGetLastError();
     return FNUM_ERR_CUDA;
   }
   const int nx = desc->n_x, nz = desc->n_z, ne = desc->n_elements, na = n_angles, nt = desc->n_samples;
-  if (!desc->positions_x || !desc->positions_z || nx < 1 || nz < 1) return FNUM_ERR_ARGUMENT;
-  if (ne < 2 || ne > 4096 || nt < 2) return FNUM_ERR_RF_DATA;
-  for (int a = 0; a < na; ++a)
-    if (!(steering_angles[a] > -M_PI / 2 && steering_angles[a] < M_PI / 2)) return FNUM_ERR_STEERING_ANGLE;
   const double fs = desc->f_s, pitch = desc->element_pitch, width = desc->element_width, c = desc->c_0;
-  if (!(fs > 0)) return FNUM_ERR_SAMPLING_RATE;
-  if (!(width > 0 && isfinite(width))) return FNUM_ERR_ELEMENT_WIDTH;
-  if (!(pitch > width && isfinite(pitch))) return FNUM_ERR_ELEMENT_PITCH;
-  if (!(c > 0 && isfinite(c))) return FNUM_ERR_SOUND_SPEED;
   const int wid = desc->window.id;
-  if (!(wid == FNUM_WINDOW_BOXCAR || wid == FNUM_WINDOW_HANN || wid == FNUM_WINDOW_TUKEY ||
-        wid == FNUM_WINDOW_TRIANGULAR) ||
-      !(desc->window.parameter >= 0 && desc->window.parameter <= 1) ||
-      (wid == FNUM_WINDOW_TUKEY && !(desc->window.parameter > 0)))
-    return FNUM_ERR_WINDOW;
-  if (desc->normalization < 0 || desc->normalization > 2) return FNUM_ERR_NORMALIZATION;
 
-  // band (the library's own band logic) and F table
-  int N = 0, k_lb = 0, k_ub = 0;
-  int s = fnum_band(desc->positions_z, nz, nt, ne, fs, width, pitch, c, desc->f_bounds, desc->index_t0, &N, &k_lb,
-                    &k_ub);
-  if (s != FNUM_OK) return s;
-  const int K = k_ub - k_lb + 1;
-  std::vector<double> F(K);
-  if (desc->f_number_values) {
-    if (desc->n_f_number_values == 1) {
-      for (int i = 0; i < K; ++i) F[i] = desc->f_number_values[0];
-    } else if (desc->n_f_number_values == K) {
-      for (int i = 0; i < K; ++i) F[i] = desc->f_number_values[i];
-    } else {
-      return FNUM_ERR_F_NUMBER;
-    }
-  } else {
-    std::vector<double> pl(K);
-    for (int i = 0; i < K; ++i) pl[i] = pitch * (k_lb + i) * fs / ((double)N * c);
-    if (fnum_f_number_values(&desc->f_number, pl.data(), K, F.data()) != FNUM_OK) return FNUM_ERR_F_NUMBER;
-  }
-  bool mono = true;
-  for (int i = 0; i < K; ++i) {
-    if (!(F[i] >= 0 && F[i] <= DBL_MAX)) return FNUM_ERR_F_NUMBER;
-    if (i > 0) {
-      const double a0 = ((float)F[i - 1] > FLT_EPSILON) ? F[i - 1] : 0.0, a1 = ((float)F[i] > FLT_EPSILON) ? F[i] : 0.0;
-      if (a1 < a0) mono = false;
-    }
-  }
-
-  // host tables (same definitions as the plan path)
-  const double M = (ne - 1.0) / 2.0, Ku = fs / ((double)N * c);
-  std::vector<dfl> col_u(nx), col_p(nx), col_m(nx), row_u2(nz), row_p(nz), el_u(ne), el_m(ne), el_lb(ne), el_ub(ne),
-      ax((size_t)na * nx), az((size_t)na * nz), g(K);
-  std::vector<int> emid(nx);
-  std::vector<double> ctr(ne);
-  for (int e = 0; e < ne; ++e) ctr[e] = pitch * (e - M);
-  for (int i = 0; i < nx; ++i) {
-    const double x = desc->positions_x[i];
-    col_u[i] = to_df(Ku * x);
-    col_p[i] = to_df(M + x / pitch);
-    col_m[i] = to_df(x);
-    int em = ne;
-    for (int e = 0; e < ne; ++e)
-      if (ctr[e] >= x) { em = e; break; }
-    emid[i] = em;
-  }
-  for (int j = 0; j < nz; ++j) {
-    const double zu = Ku * desc->positions_z[j];
-    const double hi = zu * zu, lo = fma(zu, zu, -hi);
-    const float h = (float)hi;
-    row_u2[j] = make_float2(h, (float)((hi - (double)h) + lo));
-    row_p[j] = to_df(desc->positions_z[j] / pitch);
-  }
-  for (int e = 0; e < ne; ++e) {
-    el_u[e] = to_df(Ku * ctr[e]);
-    el_m[e] = to_df(ctr[e]);
-    el_lb[e] = to_df(ctr[e] - width / 2.0);
-    el_ub[e] = to_df(ctr[e] + width / 2.0);
-  }
-  for (int a = 0; a < na; ++a) {
-    const double ex = -sin(steering_angles[a]), ez = cos(steering_angles[a]);
-    const double xref = (ex >= 0) ? -M * pitch : M * pitch;
-    for (int i = 0; i < nx; ++i) ax[(size_t)a * nx + i] = to_df(Ku * ex * (desc->positions_x[i] - xref) + desc->index_t0 / N);
-    for (int j = 0; j < nz; ++j) az[(size_t)a * nz + j] = to_df(Ku * ez * desc->positions_z[j]);
-  }
-  for (int i = 0; i < K; ++i) g[i] = ((float)F[i] > FLT_EPSILON) ? to_df(1.0 / (2.0 * F[i])) : make_float2(-1.0f, 0.0f);
+  // band, F table and the kernels' tables: the plan path's definitions
+  fnum::Band b;
+  if ((s = fnum::compute_band(desc->positions_z, nz, nt, ne, fs, width, pitch, c, desc->f_bounds, desc->index_t0,
+                              &b)) != FNUM_OK)
+    return s;
+  const int N = b.N, k_lb = b.k_lb, k_ub = b.k_ub, K = b.K;
+  std::vector<double> F;
+  if ((s = fnum::band_f_table(&desc->f_number, desc->f_number_values, desc->n_f_number_values, b, pitch, fs, c,
+                              FNUM_ERR_F_NUMBER, F)) != FNUM_OK)
+    return s;
+  const bool mono = fnum::f_monotone(F);
+  const double Ku = fs / ((double)N * c);
+  fnum::GeomTables gt;
+  fnum::build_geometry(desc->positions_x, nx, desc->positions_z, nz, ne, width, pitch, Ku, b.M, gt);
+  std::vector<dfl> ax, az, g;
+  fnum::build_tx_tables(desc->positions_x, nx, desc->positions_z, nz, steering_angles, na, Ku, b.M, pitch,
+                        desc->index_t0, N, ax, az);
+  fnum::g_table(F, g);
+  const std::vector<dfl>&col_u = gt.col_u, &col_p = gt.col_p, &col_m = gt.col_m, &row_u2 = gt.row_u2,
+                  &row_p = gt.row_p, &el_u = gt.el_u, &el_m = gt.el_m, &el_lb = gt.el_lb, &el_ub = gt.el_ub;
+  const std::vector<int>& emid = gt.col_emid;
 
   // carve the scratch array
   unsigned char* base = nullptr;
@@ -185,7 +123,7 @@ extern "C" int fnum_das_pw_noalloc(const fnum_pw_desc* desc, const double* steer
   D.nx = nx; D.nz = nz; D.ne = ne; D.na = na; D.K = K; D.k_lb = k_lb; D.k_ub = k_ub; D.N_dft = N;
   D.window_id = wid; D.window_par = (float)desc->window.parameter;
   D.norm = desc->normalization != FNUM_NORMALIZATION_OFF;
-  D.seg_cap = (mono ? (K < 2 * ne + 16 ? K : 2 * ne + 16) : K) + 1;  // + the sentinel entry
+  D.seg_cap = (mono ? std::min(K, 2 * ne + 16) : K) + 1;  // + the sentinel entry, as the plan path
   D.flush_chunks = 4;
   D.scale = (float)(2.0 / N);
   D.pitch_f = (float)pitch;  // element spacing of the closed-form aperture sums

@@ -472,6 +472,17 @@ class _Plan:
         _lib.check(_lib.lib().fnum_plan_execute_dft(self._ptr, rf.data_ptr(), int(rf.dtype == torch.float64),
                                                     self._stream_ptr(stream)), self._saft)
 
+    def spectra(self, stream=None):
+        """Band spectra of the last execute (fnum_plan_spectra): complex64 tensor,
+        plane wave [n_elements, n_bins, n_angles], SAFT [n_tx, n_rx, n_bins]."""
+        import torch
+        inf = self.info()
+        shape = ((inf["n_elements"], inf["n_elements"], inf["n_bins"]) if self._saft else
+                 (inf["n_elements"], inf["n_bins"], inf["n_angles"]))
+        out = torch.empty(shape, dtype=torch.complex64, device=torch.device("cuda", self.device))
+        _lib.check(_lib.lib().fnum_plan_spectra(self._ptr, out.data_ptr(), self._stream_ptr(stream)), self._saft)
+        return out
+
     def execute_beamform(self, out, weights=None, weights_rx=None, stream=None):
         _lib.check(_lib.lib().fnum_plan_execute_beamform(
             self._ptr, out.data_ptr(), weights.data_ptr() if weights is not None else None,
@@ -537,6 +548,7 @@ class PWPlan(_Plan):
         _lib.check(_lib.lib().fnum_pw_plan_create(_lib.C.byref(d), _lib.dptr(self._angles), self._angles.size, flags,
                                                   _lib.C.byref(ptr)))
         self._ptr = ptr
+        self.device = int(device)
         inf = self.info()
         self.n_x, self.n_z, self.n_bins = inf["n_x"], inf["n_z"], inf["n_bins"]
         self.n_elements, self.n_angles = inf["n_elements"], inf["n_angles"]
@@ -584,8 +596,35 @@ def _pw_sharpness_grad(self, rf, grad_spectra=True, stream=None):
     return L.value, dc.value, g
 
 
+def _pw_set_spectra(self, spectra, stream=None):
+    """Loads band spectra (complex64 CUDA tensor [n_elements, n_bins, n_angles]) into
+    the plan (fnum_plan_set_spectra), for execute_beamform or adjoint."""
+    import torch
+    if spectra.dtype != torch.complex64 or not spectra.is_cuda or not spectra.is_contiguous():
+        raise ValueError("spectra must be a contiguous complex64 CUDA tensor")
+    if tuple(spectra.shape) != (self.n_elements, self.n_bins, self.n_angles):
+        raise ValueError("spectra must have shape [n_elements, n_bins, n_angles]")
+    _lib.check(_lib.lib().fnum_plan_set_spectra(self._ptr, spectra.data_ptr(), self._stream_ptr(stream)))
+
+
+def _pw_adjoint(self, cotangent, dc=True, stream=None):
+    """Adjoint of the compounded beamformer (fnum_pw_adjoint): for G = dL/dI*
+    (complex64 CUDA tensor [N_x, N_z]) at the plan's current spectra and sound
+    speed, returns (dL/dX* as a complex64 tensor [n_elements, n_bins, n_angles],
+    dL/dc or None)."""
+    import torch
+    cot = cotangent.reshape(self.n_x, self.n_z).to(torch.complex64).contiguous()
+    g = torch.empty((self.n_elements, self.n_bins, self.n_angles), dtype=torch.complex64, device=cot.device)
+    v = _lib.C.c_double(0.0)
+    _lib.check(_lib.lib().fnum_pw_adjoint(self._ptr, cot.data_ptr(), g.data_ptr(), _lib.C.byref(v) if dc else None,
+                                          self._stream_ptr(stream)))
+    return g, (v.value if dc else None)
+
+
 PWPlan.set_sound_speed = _pw_set_sound_speed
 PWPlan.sharpness_grad = _pw_sharpness_grad
+PWPlan.set_spectra = _pw_set_spectra
+PWPlan.adjoint = _pw_adjoint
 
 
 class SAPlan(_Plan):
@@ -618,6 +657,7 @@ class SAPlan(_Plan):
         ptr = _lib.C.c_void_p()
         _lib.check(_lib.lib().fnum_sa_plan_create(_lib.C.byref(d), flags, _lib.C.byref(ptr)), True)
         self._ptr = ptr
+        self.device = int(device)
         inf = self.info()
         self.n_x, self.n_z, self.n_bins = inf["n_x"], inf["n_z"], inf["n_bins"]
         self.n_out = 1

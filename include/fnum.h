@@ -162,6 +162,18 @@ typedef struct fnum_pw_desc {
 int fnum_das_pw(const fnum_pw_desc* desc, const double* steering_angles, int n_angles,
                 const double* data_rf, int flags, float* image_re, float* image_im, float* weights);
 
+/* Sharpness-loss gradients from host buffers (no counterpart in the reference,
+   which has no derivatives): the compounded image of all n_angles (data_rf as
+   for fnum_das_pw), its loss L = -sum|I|^4 / (sum|I|^2)^2, dL/dc at desc->c_0
+   (band, F table and apertures held at that speed) and, if grad_re / grad_im
+   are not NULL, the Wirtinger gradient dL/dX* of the band spectra as separate
+   real / imaginary planes [n_angles][n_elements][n_bins] (bins fastest:
+   MATLAB's N_bins x N_el x N_angles).  Shares fnum_das_pw's plan cache.  The
+   MATLAB binding is f_number_gb300/mex/gpu_bf_das_pw_sharpness_grad.cpp. */
+int fnum_das_pw_sharpness_grad(const fnum_pw_desc* desc, const double* steering_angles, int n_angles,
+                               const double* data_rf, double* loss, double* dloss_dc, float* grad_re,
+                               float* grad_im);
+
 /* --- synthetic aperture (das_sa) ---------------------------------------- */
 typedef struct fnum_sa_desc {
   const double* positions_x; int n_x;
@@ -209,10 +221,23 @@ int fnum_plan_execute(fnum_plan* plan, const void* d_rf, int rf_is_double, void*
                       float* d_weights, float* d_weights_rx, void* stream);
 /* the band stage alone: d_rf -> d_spectra (plan-internal), for timing */
 int fnum_plan_execute_dft(fnum_plan* plan, const void* d_rf, int rf_is_double, void* stream);
+/* copies the band spectra of the last execute (or execute_dft) to d_spectra
+   (device float2; plane wave [n_elements][n_bins][n_angles], synthetic aperture
+   [n_tx][n_rx][n_bins]), stream-ordered.  No counterpart in the reference,
+   whose spectra live only inside a gateway call. */
+int fnum_plan_spectra(const fnum_plan* plan, void* d_spectra, void* stream);
 /* the beamforming stage alone on the spectra of the last fnum_plan_execute_dft */
 int fnum_plan_execute_beamform(fnum_plan* plan, void* d_image, float* d_weights, float* d_weights_rx,
                                void* stream);
 int fnum_plan_info_get(const fnum_plan* plan, fnum_plan_info* info);
+
+/* Plans of the two host-buffer entry points above are cached by the VALUES of
+   their arguments (never the addresses of the caller's arrays), up to 4 per
+   entry point, least recently used first out.  No counterpart in the reference
+   (which allocates and frees per call).  plans_created counts the plans an
+   entry point has built (saft = 0: fnum_das_pw, 1: fnum_das_sa); plans_cached
+   is the number it holds now.  Either pointer may be NULL. */
+int fnum_host_cache_info(int saft, long long* plans_created, int* plans_cached);
 
 /* --- plane wave without device allocation ------------------------------- */
 /* No counterpart in the reference (whose gateways allocate and free device
@@ -231,7 +256,9 @@ int fnum_plan_info_get(const fnum_plan* plan, fnum_plan_info* info);
      flags     0 or FNUM_FLAG_COMPOUND
    The first call on a device looks up the array's device address (once per
    device, with that device current): make that first call before any stream
-   capture.  Problems whose tables, spectra and one block of aperture segments
+   capture, and do not reset the device (cudaDeviceReset, MATLAB's
+   reset(gpuDevice)) between calls, since the address is kept.  Arguments are
+   checked as fnum_das_pw checks them, with the same status codes.  Problems whose tables, spectra and one block of aperture segments
    do not fit return FNUM_ERR_NOALLOC_TOO_LARGE; larger ones run with as many
    resident blocks as fit.  All calls share the array and it keeps the last
    call's contents; everything that must start at zero is cleared per call.
@@ -298,6 +325,22 @@ int fnum_pw_plan_set_sound_speed(fnum_plan* plan, double c_0);
    among them).  Synchronises `stream`. */
 int fnum_pw_sharpness_grad(fnum_plan* plan, const void* d_rf, int rf_is_double, double* loss, double* dloss_dc,
                            void* d_grad_spectra, void* stream);
+
+/* The adjoint of a compounded plane-wave plan's beamformer, for any real loss L
+   of its image I (no counterpart in the reference).  d_cotangent holds
+   dL/dI* per voxel (device float2 [n_x][n_z], the image layout); the call
+   returns, for the plan's current spectra X (those of the last execute, or of
+   fnum_plan_set_spectra) and sound speed, the Wirtinger gradient dL/dX* (device
+   float2 [n_elements][n_bins][n_angles]; NULL keeps it in the plan) and, if
+   dloss_dc is not NULL, dL/dc = 2 Re sum_v conj(dL/dI*_v) dI_v/dc with the band,
+   F table and apertures held fixed.  I is linear in X, so dL/dX* = A^H dL/dI*
+   for the beamformer A.  Allocates the plan's gradient buffers on first use;
+   synchronises `stream`. */
+int fnum_pw_adjoint(fnum_plan* plan, const void* d_cotangent, void* d_grad_spectra, double* dloss_dc, void* stream);
+/* loads band spectra (device float2, the layout of fnum_plan_spectra) into the
+   plan, e.g. to beamform spectra a caller produced (fnum_plan_execute_beamform)
+   or to take fnum_pw_adjoint at them.  No counterpart in the reference. */
+int fnum_plan_set_spectra(fnum_plan* plan, const void* d_spectra, void* stream);
 
 /* copies the plan's F table (n_bins values; two tables for SA: tx then rx) */
 int fnum_plan_f_numbers(const fnum_plan* plan, double* values);

@@ -4,8 +4,10 @@ TEST INFRASTRUCTURE ONLY.
 * oracle/liboracle.so: the C restatement (gcc + OpenMP; portable C, builds on
   x86_64 and aarch64).
 * oracle/_ref/ref_kernels.fatbin: the reference's own CUDA kernels compiled
-  from their sources under /root/reference/+cuda (device code for sm_103a
-  only; built where the reference is mounted, then shipped with the tree).
+  from their sources in the reference checkout's +cuda directory (device code
+  for sm_103a only; built where the reference is mounted, then shipped with the
+  tree).  The checkout is $FNUM_REFERENCE_ROOT, or ``--reference DIR``; its
+  default is where this build environment mounts it.
 * oracle/_ref/libref_harness.so: the project-written host driver that runs
   those kernels with the MEX host sequence (nvcc; built wherever the fatbin
   and a CUDA toolkit are present).
@@ -23,7 +25,8 @@ SRC = os.path.join(HERE, "fnum_oracle.c")
 REF_DIR = os.path.join(HERE, "_ref")
 FATBIN = os.path.join(REF_DIR, "ref_kernels.fatbin")
 HARNESS = os.path.join(REF_DIR, "libref_harness.so")
-REFERENCE_CUDA = "/root/reference/+cuda"
+REFERENCE_ROOT = os.environ.get("FNUM_REFERENCE_ROOT", "/root/reference")
+REFERENCE_CUDA = os.path.join(REFERENCE_ROOT, "+cuda")
 TU = os.path.join(HERE, "ref_harness", "ref_kernels_tu.cu")
 DRIVER = os.path.join(HERE, "ref_harness", "ref_driver.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -52,15 +55,16 @@ def build_c(force=False):
     return LIB
 
 
-def build_ref(force=False):
+def build_ref(force=False, reference_cuda=None):
     """Reference kernels (only where the reference sources are mounted) and the
     harness driver (wherever the fatbin exists).  Returns the harness path or None."""
     nv = _nvcc()
     if nv is None:
         return None
+    ref_cuda = reference_cuda or REFERENCE_CUDA
     os.makedirs(REF_DIR, exist_ok=True)
-    if os.path.isdir(REFERENCE_CUDA) and (force or _stale(FATBIN, TU)):
-        _run([nv, "-fatbin"] + ARCH + ["-I", REFERENCE_CUDA, TU, "-o", FATBIN])
+    if os.path.isdir(ref_cuda) and (force or _stale(FATBIN, TU)):
+        _run([nv, "-fatbin"] + ARCH + ["-I", ref_cuda, TU, "-o", FATBIN])
     if not os.path.exists(FATBIN):
         return None
     if force or _stale(HARNESS, DRIVER):
@@ -69,14 +73,17 @@ def build_ref(force=False):
     return HARNESS
 
 
-def build(force=False):
+def build(force=False, reference_root=None):
     build_c(force)
     try:
-        build_ref(force)
+        build_ref(force, os.path.join(reference_root, "+cuda") if reference_root else None)
     except RuntimeError as e:  # the checker's optional half: report, do not stop the product build
         sys.stderr.write("reference harness not built: %s\n" % e)
     return LIB
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv))
+    root = None
+    if "--reference" in sys.argv:
+        root = sys.argv[sys.argv.index("--reference") + 1]
+    print(build(force="--force" in sys.argv, reference_root=root))

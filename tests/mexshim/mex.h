@@ -1,16 +1,26 @@
-/* Declarations of the MATLAB MEX C API used by the gateways in
-   f_number_gb300/mex (signature check only: the functions are provided by
-   MATLAB at link time).  Separate-complex API (mxGetImagData). */
+/* The part of the MATLAB MEX C API (separate-complex, mxGetImagData) that the
+   gateways in f_number_gb300/mex use.  MATLAB is not present here: these are
+   implemented by tests/mexshim/mexshim.cpp, a minimal stand-in that lets the
+   gateways run under the tests.  mexErrMsgIdAndTxt does not return (the shim
+   throws, as MATLAB longjmps out of the gateway). */
 #pragma once
 #include <stddef.h>
 #include <stdio.h>
 typedef struct mxArray_tag mxArray;
 typedef size_t mwSize;
 typedef enum { mxREAL, mxCOMPLEX } mxComplexity;
-typedef enum { mxUNKNOWN_CLASS, mxDOUBLE_CLASS = 6, mxSINGLE_CLASS = 7 } mxClassID;
+typedef enum {
+  mxUNKNOWN_CLASS = 0,
+  mxCHAR_CLASS = 4,
+  mxLOGICAL_CLASS = 3,
+  mxDOUBLE_CLASS = 6,
+  mxSINGLE_CLASS = 7,
+  mxOBJECT_CLASS = 18
+} mxClassID;
 #ifdef __cplusplus
 extern "C" {
 #endif
+void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]);
 void mexErrMsgIdAndTxt(const char* id, const char* fmt, ...);
 int mexCallMATLAB(int nlhs, mxArray* plhs[], int nrhs, mxArray* prhs[], const char* name);
 bool mxIsDouble(const mxArray*);
@@ -33,6 +43,7 @@ mxArray* mxDuplicateArray(const mxArray*);
 mxArray* mxCreateString(const char*);
 mxArray* mxCreateDoubleMatrix(mwSize, mwSize, mxComplexity);
 mxArray* mxCreateNumericMatrix(mwSize, mwSize, mxClassID, mxComplexity);
+mxArray* mxCreateNumericArray(mwSize, const mwSize*, mxClassID, mxComplexity);
 void mxDestroyArray(mxArray*);
 #ifdef __cplusplus
 }

@@ -32,6 +32,7 @@ def rel_l2_finite(a, ref):
 
 
 PW = load("ref_pw")
+PWM = load("ref_pw_multi")
 SA = load("ref_sa")
 
 
@@ -73,3 +74,20 @@ def test_oracle_matches_reference_sa(i):
         assert rel_l2_finite(img, ref) < TOL_REF
     np.testing.assert_allclose(wt, d["%d_wtx" % i], rtol=1e-5)
     np.testing.assert_allclose(wr, d["%d_wrx" % i], rtol=1e-5)
+
+
+@pytest.mark.parametrize("i", range(len(PWM[1]["cases"])), ids=[c["name"] for c in PWM[1]["cases"]])
+def test_oracle_matches_reference_pw_compounded(i):
+    """Compounded plane waves: the golden image is the sum of the reference's
+    per-angle gateway images (one angle per call, das_pw.m:298)."""
+    from oracle import coracle as CO
+    d, m = PWM
+    c, a = m["cases"][i], m["array"]
+    px, pz = np.array(m["positions_x"]), np.array(m["positions_z"])
+    rf = d["%d_rf" % i].astype(np.float64)                                       # [A, E, T]
+    ix, iz = np.meshgrid(np.arange(px.size), np.arange(pz.size), indexing="ij")
+    img, w, _ = CO.pw_mex(px, pz, rf, m["f_s"], d["%d_angles" % i], a["width"], a["pitch"], m["c"],
+                          tuple(c["f_bounds"]), c["t0"], tuple(c["window"]), c["F"], c["norm"], ix.ravel(), iz.ravel())
+    img = img.reshape(px.size, pz.size).T
+    assert rel_l2_finite(img, d["%d_image" % i]) < TOL_REF
+    np.testing.assert_allclose(w.reshape(px.size, pz.size).T, d["%d_weights" % i], rtol=1e-5, atol=1e-6)

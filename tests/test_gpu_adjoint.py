@@ -78,3 +78,67 @@ def test_sharpness_gradients_match_finite_differences(gpu):
     Lm = plan.sharpness_grad(torch.tensor(rf - eps * d_rf, dtype=torch.float32, device=gpu), grad_spectra=False)[0]
     assert abs((Lp - Lm) / (2 * eps) - an) <= 2 * TOL_FD * abs(an)
     plan.close()
+
+
+def test_adjoint_inner_product_identity(gpu):
+    """fnum_pw_adjoint is the adjoint of the beamformer: for random spectra dX and a
+    random image cotangent G, Re <G, A dX> = Re <A^H G, dX> (A linear in X)."""
+    import torch
+    plan, rf, rf_d, (arr, px, pz, angles, rng) = _case(gpu, seed=7)
+    plan.execute(rf_d)
+    shape = (plan.n_elements, plan.n_bins, plan.n_angles)
+    dX = torch.tensor(rng.standard_normal(shape) + 1j * rng.standard_normal(shape), dtype=torch.complex64,
+                      device=gpu)
+    G = torch.tensor(rng.standard_normal((plan.n_x, plan.n_z)) + 1j * rng.standard_normal((plan.n_x, plan.n_z)),
+                     dtype=torch.complex64, device=gpu)
+    plan.set_spectra(dX)
+    img = torch.empty((1, plan.n_x, plan.n_z), dtype=torch.complex64, device=gpu)
+    plan.execute_beamform(img)
+    gX, _ = plan.adjoint(G, dc=False)
+    lhs = torch.sum(torch.conj(G.to(torch.complex128)) * img[0].to(torch.complex128)).real.item()
+    rhs = torch.sum(torch.conj(gX.to(torch.complex128)) * dX.to(torch.complex128)).real.item()
+    scale = torch.linalg.vector_norm(G.abs().double()).item() * torch.linalg.vector_norm(img.abs().double()).item()
+    assert abs(lhs - rhs) <= 1e-5 * scale, (lhs, rhs, scale)
+    plan.close()
+
+
+def test_autograd_function_matches_abi_and_finite_differences(gpu):
+    """f_number_gb300.autograd.pw_beamform: torch autograd through the C ABI.  The
+    sharpness loss written in torch gives the gradients of fnum_pw_sharpness_grad
+    (torch's complex grad is 2 dL/dX*), and a second, non-sharpness loss (a
+    weighted image energy) matches central differences in c and along a random
+    spectra direction."""
+    import torch
+    from f_number_gb300 import autograd as AG
+    plan, rf, rf_d, (arr, px, pz, angles, rng) = _case(gpu, seed=8)
+    plan.set_sound_speed(1510.0)
+    L_abi, dc_abi, g_abi = plan.sharpness_grad(rf_d)
+    X = plan.spectra().clone().requires_grad_(True)
+    c = torch.tensor(1510.0, dtype=torch.float64, requires_grad=True)
+    L = AG.sharpness(AG.pw_beamform(plan, X, c))
+    L.backward()
+    assert abs(L.item() - L_abi) <= TOL_LOSS * abs(L_abi)
+    assert abs(c.grad.item() - dc_abi) <= TOL_DC * abs(dc_abi), (c.grad.item(), dc_abi)
+    assert (torch.linalg.vector_norm(X.grad - 2 * g_abi) / torch.linalg.vector_norm(2 * g_abi)).item() < TOL_GX
+
+    wv = torch.tensor(rng.uniform(0.5, 1.5, (plan.n_x, plan.n_z)), device=gpu)
+
+    def energy(Xv, cv):
+        img = AG.pw_beamform(plan, Xv, cv)
+        return (wv * (img.real.double() ** 2 + img.imag.double() ** 2)).sum()
+
+    X0 = X.detach().clone()
+    Xr = X0.clone().requires_grad_(True)
+    cr = torch.tensor(1510.0, dtype=torch.float64, requires_grad=True)
+    E = energy(Xr, cr)
+    E.backward()
+    h = 0.2
+    fd_c = (energy(X0, 1510.0 + h).item() - energy(X0, 1510.0 - h).item()) / (2 * h)
+    assert abs(fd_c - cr.grad.item()) <= TOL_FD * abs(cr.grad.item()), (fd_c, cr.grad.item())
+    d = torch.tensor(rng.standard_normal(X0.shape) + 1j * rng.standard_normal(X0.shape), dtype=torch.complex64,
+                     device=gpu) * X0.abs().mean()
+    eps = 1e-2
+    fd_x = (energy(X0 + eps * d, 1510.0).item() - energy(X0 - eps * d, 1510.0).item()) / (2 * eps)
+    an = torch.sum(torch.conj(Xr.grad.to(torch.complex128)) * d.to(torch.complex128)).real.item()
+    assert abs(fd_x - an) <= TOL_FD * abs(an), (fd_x, an)
+    plan.close()

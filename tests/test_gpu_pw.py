@@ -244,3 +244,41 @@ def test_single_angle_full_size_sampled(gpu):
                              wl.c, wl.f_bounds, 0.0, win.spec(), fn.spec(), "on", ix, iz)
     assert rel_l2(img[iz, ix], ref) < TOL_L2
     np.testing.assert_allclose(w[iz, ix], wref, rtol=TOL_W)
+
+
+def test_host_plan_cache_keys_on_values(gpu):
+    """The host-buffer gateway keeps its plans by argument values: equal geometry
+    in fresh arrays (as MATLAB passes temporaries) reuses the plan; alternating
+    between two geometries keeps both."""
+    import ctypes as C
+    from f_number_gb300 import _lib
+    L = _lib.lib()
+
+    def created():
+        n = C.c_longlong(0)
+        L.fnum_host_cache_info(0, C.byref(n), None)
+        return n.value
+
+    arr = synth.LinearArray(32, 0.3048e-3, 0.918 * 0.3048e-3)
+    rng = np.random.default_rng(11)
+    sc = synth.random_points(rng, 3, (-2e-3, 2e-3), (6e-3, 10e-3))
+    rf = synth.pw_rf(rng, arr, sc, [0.0], 400, 20e6, 1540.0)[0].T
+    win, fn = windows.hann(), f_numbers.grating.angle_lb(60.0, 1.5)
+
+    def call(nx):
+        px = np.linspace(-2e-3, 2e-3, nx)            # a fresh array on every call
+        pz = np.linspace(6e-3, 10e-3, 9)
+        return das.gpu_bf_das_pw_rf(px, pz, rf.copy(), 20e6, 0.0, arr.width, arr.pitch, 1540.0, [2e6, 7e6], 0, win,
+                                    fn, normalizations.on(), 0)
+
+    first = call(7)[0]
+    n0 = created()
+    again = call(7)[0]
+    assert created() == n0                      # same values, new arrays: no new plan
+    np.testing.assert_array_equal(first, again)
+    call(8)
+    n1 = created()
+    assert n1 == n0 + 1
+    call(7)
+    call(8)
+    assert created() == n1                      # both geometries stay cached
