@@ -691,12 +691,37 @@ def run_adjoint(args):
     plan.execute(rf, out=img, stream=stream)
     b.record(stream)
     torch.cuda.synchronize()
+    fwd_ms = a.elapsed_time(b)
+    # the adjoint alone (fnum_pw_adjoint: dL/dX* and dL/dc for a cotangent) on the frame's spectra
+    cot = torch.randn((plan.n_x, plan.n_z), dtype=torch.complex64, device=dev)
+    plan.adjoint(cot, stream=stream)
+    adj = []
+    for _ in range(3):
+        a.record(stream)
+        plan.adjoint(cot, stream=stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        adj.append(a.elapsed_time(b))
+    adj_ms = float(np.mean(adj))
+    info = plan.info()
+    from f_number_gb300 import _lib
+    peak = _lib.C.c_double(0.0)
+    _lib.check(_lib.lib().fnum_diag_fp32_peak(0, _lib.C.byref(peak)))
+    # per active voxel x element x bin x angle term the adjoint forms two complex MACs:
+    # dL/dX* and the dL/dc sum H (16 FLOP)
+    adj_tflops = 16.0 * info["active_terms"] / (adj_ms * 1e-3) / 1e12
+    roof = {"bound": "fp32", "achieved": adj_tflops, "peak": peak.value, "unit": "TFLOP/s",
+            "frac": adj_tflops / peak.value if peak.value else None, "traffic": None,
+            "kernel": "pw_adjoint_kernel (+ dL/dc reduction)",
+            "work": "16 FLOP per active term (two complex MACs: dL/dX* and H); %d active terms"
+                    % info["active_terms"],
+            "peak_source": "measured FP32 FMA throughput (fnum_diag_fp32_peak)"}
     out = {"metric": ADJ_METRIC, "value": args.steps / dt, "unit": "evaluations/s", "n_gpus": 1, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32 (double-float phase, FP64 reductions)", "data": "synthetic",
            "config": {"workload": "adjoint_cpwc_11angles_128el_2048smp_%dx%d_rf_at_1500" % (args.grid, args.grid),
                       "trial_c": 1500.0, "frozen_at_c": 1540.0},
-           "forward_ms": a.elapsed_time(b), "sweep": sweep, "clocks": clk}
+           "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "roofline": roof, "sweep": sweep, "clocks": clk}
     print(json.dumps(out))
     plan.close()
 

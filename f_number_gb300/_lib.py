@@ -20,9 +20,10 @@ EXPORTS = (
     "fnum_batch_frame_times", "fnum_batch_destroy", "fnum_pw_plan_set_sound_speed", "fnum_pw_sharpness_grad",
     "fnum_plan_m_signal", "fnum_plan_set_kernel_variant", "fnum_diag_mma_f16_peak", "fnum_host_cache_info",
     "fnum_plan_spectra", "fnum_pw_adjoint", "fnum_plan_set_spectra", "fnum_das_pw_sharpness_grad",
+    "fnum_batch_info", "fnum_plan_set_shape",
 )
 
-ABI_VERSION = 3   # FNUM_ABI_VERSION of include/fnum.h
+ABI_VERSION = 4   # FNUM_ABI_VERSION of include/fnum.h
 
 # status codes (fnum_status)
 OK = 0
@@ -98,7 +99,7 @@ class PlanInfo(C.Structure):
         ("scratch_bytes", C.c_longlong),
         ("scale", C.c_double),
         ("executed_terms", C.c_longlong),
-        ("kernel_variant", C.c_int), ("grid", C.c_int),
+        ("kernel_variant", C.c_int), ("grid", C.c_int), ("blocks_per_sm", C.c_int), ("bin_chunk", C.c_int),
     ]
 
 
@@ -179,6 +180,10 @@ def lib():
     L.fnum_batch_execute.argtypes = [C.c_void_p, C.c_void_p]
     L.fnum_batch_frame_times.restype = C.c_int
     L.fnum_batch_frame_times.argtypes = [C.c_void_p, _fp]
+    L.fnum_plan_set_shape.restype = C.c_int
+    L.fnum_plan_set_shape.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    L.fnum_batch_info.restype = C.c_int
+    L.fnum_batch_info.argtypes = [C.c_void_p, _ip, _ip]
     L.fnum_batch_destroy.restype = C.c_int
     L.fnum_batch_destroy.argtypes = [C.c_void_p]
     L.fnum_pw_plan_set_sound_speed.restype = C.c_int

@@ -1192,6 +1192,16 @@ int fnum_plan_info_get(const fnum_plan* plan, fnum_plan_info* info) {
   info->executed_terms = (long long)c[4];
   info->kernel_variant = plan->kind == 0 ? fnum::pw_variant_of(plan->pw) : 0;
   info->grid = plan->grid;
+  info->blocks_per_sm = 0;
+  info->bin_chunk = 0;
+  if (plan->kind == 0 && !plan->pw.m_sem) {
+    int bps = 0;
+    (void)fnum::pw_fused_grid(plan->pw, &bps);
+    info->blocks_per_sm = bps;
+    info->bin_chunk = fnum::pw_variant_of(plan->pw) == fnum::TC_VARIANT
+                          ? ((plan->pw.tc_tb > 0 && plan->pw.tc_tb < 32) ? plan->pw.tc_tb : 32)
+                          : plan->pw.flush_chunks * fnum::KCHUNK;
+  }
   if ((c[2] & fnum::ERR_SEG_OVERFLOW) || (c[5] & fnum::ERR_DFT_TIMEOUT)) return FNUM_ERR_INTERNAL;
   return FNUM_OK;
 }
@@ -1340,9 +1350,31 @@ int fnum_plan_autotune(fnum_plan* plan, const void* d_rf, int rf_is_double, int*
   float2* img = nullptr;
   int s = FNUM_OK;
   const size_t n_img = (size_t)plan->n_out * plan->pw.nx * plan->pw.nz;
-  const int v0 = plan->pw.variant, g0 = plan->grid;
+  const fnum::PWDev d0 = plan->pw;
+  const int g0 = plan->grid;
   float best = 3.0e38f;
-  int best_v = fnum::pw_variant_of(plan->pw), best_g = plan->grid;
+  fnum::PWDev best_d = plan->pw;
+  int best_g = plan->grid;
+  // times the plan's current variant and shape (a warm-up, then two beamforms)
+  auto trial = [&]() -> int {
+    plan->grid = std::min(fnum::pw_fused_grid(plan->pw, nullptr), plan->max_grid);
+    int st2 = plan_beamform(plan, img, nullptr, nullptr, st);
+    if (st2) return st2;
+    float t = 0.0f;
+    cudaError_t e2 = cudaEventRecord(e0, st);
+    for (int r = 0; r < 2 && e2 == cudaSuccess && !st2; ++r) st2 = plan_beamform(plan, img, nullptr, nullptr, st);
+    if (st2) return st2;
+    if (e2 == cudaSuccess) e2 = cudaEventRecord(e1, st);
+    if (e2 == cudaSuccess) e2 = cudaEventSynchronize(e1);
+    if (e2 == cudaSuccess) e2 = cudaEventElapsedTime(&t, e0, e1);
+    if (e2 != cudaSuccess) return cuda_status(e2);
+    if (t < best) {
+      best = t;
+      best_d = plan->pw;
+      best_g = plan->grid;
+    }
+    return FNUM_OK;
+  };
   cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&e0);
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
@@ -1352,35 +1384,43 @@ int fnum_plan_autotune(fnum_plan* plan, const void* d_rf, int rf_is_double, int*
     goto done;
   }
   if ((s = plan_dft(plan, d_rf, rf_is_double, st))) goto done;
-  for (int v = 1; v <= fnum::pw_variant_count(); ++v) {
+  // 1: the kernel variants (pass shapes) at the default launch shape
+  for (int v = 1; v <= fnum::pw_variant_count() && !s; ++v) {
+    plan->pw = d0;
     plan->pw.variant = v;
-    plan->grid = std::min(fnum::pw_fused_grid(plan->pw, nullptr), plan->max_grid);
-    if ((s = plan_beamform(plan, img, nullptr, nullptr, st))) goto done;  // warm-up
-    float t = 0.0f;
-    e = cudaEventRecord(e0, st);
-    for (int r = 0; r < 2 && e == cudaSuccess && !s; ++r) s = plan_beamform(plan, img, nullptr, nullptr, st);
-    if (s) goto done;
-    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
-    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
-    if (e != cudaSuccess) {
-      s = cuda_status(e);
-      goto done;
-    }
-    if (t < best) {
-      best = t;
-      best_v = v;
-      best_g = plan->grid;
-    }
+    plan->pw.blocks_per_sm = 0;
+    plan->pw.tc_tb = 0;
+    plan->pw.flush_chunks = 4;
+    s = trial();
+  }
+  // 2: the launch shape of the best variant: resident blocks per SM (all, or one fewer,
+  // which leaves each block more L1) and the bins between exact re-anchorings (tensor
+  // cores: 32 or 16; FP32 kernels: 4 or 2 chunks of 64 bins).  Both alternatives
+  // re-anchor at least as often, so none is less accurate than the default.
+  if (!s) {
+    const fnum::PWDev dv = best_d;
+    int bps = 0;
+    plan->pw = dv;
+    (void)fnum::pw_fused_grid(plan->pw, &bps);
+    for (int occ = 0; occ < 2 && !s; ++occ)
+      for (int ch = 0; ch < 2 && !s; ++ch) {
+        if (occ == 0 && ch == 0) continue;   // the default shape, timed above
+        if (occ == 1 && bps <= 1) continue;
+        plan->pw = dv;
+        plan->pw.blocks_per_sm = occ ? bps - 1 : 0;
+        if (fnum::pw_variant_of(dv) == fnum::TC_VARIANT) plan->pw.tc_tb = ch ? 16 : 0;
+        else plan->pw.flush_chunks = ch ? 2 : 4;
+        s = trial();
+      }
   }
 done:
   if (s) {
-    plan->pw.variant = v0;
+    plan->pw = d0;
     plan->grid = g0;
   } else {
-    plan->pw.variant = best_v;
+    plan->pw = best_d;
     plan->grid = best_g;
-    if (variant) *variant = best_v;
+    if (variant) *variant = fnum::pw_variant_of(best_d);
     if (ms) *ms = 0.5f * best;
   }
   if (img) cudaFree(img);
@@ -1391,6 +1431,25 @@ done:
   return s;
 }
 
+int fnum_plan_set_shape(fnum_plan* plan, int blocks_per_sm, int bin_chunk) {
+  if (!plan) return FNUM_ERR_ARGUMENT;
+  if (plan->kind != 0 || plan->pw.m_sem)
+    return (blocks_per_sm == 0 && bin_chunk == 0) ? FNUM_OK : FNUM_ERR_ARGUMENT;
+  if (blocks_per_sm < 0 || bin_chunk < 0) return FNUM_ERR_ARGUMENT;
+  FNUM_CUDA(cudaSetDevice(plan->device));
+  fnum::PWDev& D = plan->pw;
+  if (fnum::pw_variant_of(D) == fnum::TC_VARIANT) {
+    if (bin_chunk != 0 && bin_chunk != 16 && bin_chunk != 32) return FNUM_ERR_ARGUMENT;
+    D.tc_tb = bin_chunk;
+  } else {
+    if (bin_chunk != 0 && bin_chunk != 128 && bin_chunk != 256) return FNUM_ERR_ARGUMENT;
+    D.flush_chunks = bin_chunk == 128 ? 2 : 4;
+  }
+  D.blocks_per_sm = blocks_per_sm;
+  plan->grid = std::min(fnum::pw_fused_grid(D, nullptr), plan->max_grid);
+  return FNUM_OK;
+}
+
 struct fnum_batch {
   int device = 0;
   int n = 0;
@@ -1398,14 +1457,100 @@ struct fnum_batch {
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t start = nullptr;
   std::vector<cudaEvent_t> done;   // per frame, recorded when the frame's image is complete
+  // persistent tensor-core launches, one per window of the compounded tensor-core frames
+  struct TcGroup {
+    int window_id = 0, grid = 0;
+    std::vector<int> frames;        // batch frame indices, largest first
+    fnum::PWBatchDev dev{};
+  };
+  std::vector<TcGroup> groups;
+  std::vector<void*> allocs;
+  int persistent_frames = 0;
   ~fnum_batch() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     if (start) cudaEventDestroy(start);
     for (cudaEvent_t ev : done)
       if (ev) cudaEventDestroy(ev);
+    for (void* p : allocs) cudaFree(p);
   }
 };
+
+extern "C++" {
+namespace {
+
+// a frame that the persistent tensor-core launch can take: a compounded plane-wave plan
+// whose kernel variant is the tensor-core one
+bool tc_persistent(const fnum_plan* P) {
+  return P->kind == 0 && P->n_out == 1 && !P->pw.m_sem && !(P->flags & FNUM_FLAG_PLAIN_KERNEL) &&
+         fnum::pw_variant_of(P->pw) == fnum::TC_VARIANT && P->pw.tc_B;
+}
+
+template <typename T>
+int batch_upload(fnum_batch* B, T** dst, const std::vector<T>& v) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(v.size(), 1) * sizeof(T));
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return cuda_status(e);
+  }
+  B->allocs.push_back(q);
+  *dst = (T*)q;
+  if (!v.empty()) FNUM_CUDA(cudaMemcpy(q, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return FNUM_OK;
+}
+
+// descriptor arrays, tile prefix sums, counter and segment scratch of one persistent group
+int build_tc_group(fnum_batch* B, fnum_batch::TcGroup& G, fnum_plan* const* plans, void* const* d_images,
+                   float* const* d_weights) {
+  std::vector<fnum::PWDev> frames;
+  std::vector<float2*> images;
+  std::vector<float*> weights;
+  std::vector<int> tile_start(1, 0);
+  int max_ne = 1, seg_cap = 1;
+  for (int f : G.frames) {
+    const fnum::PWDev& D = plans[f]->pw;
+    frames.push_back(D);
+    images.push_back((float2*)d_images[f]);
+    weights.push_back(d_weights ? d_weights[f] : nullptr);
+    tile_start.push_back(tile_start.back() + fnum::pw_tc_tiles(D));
+    max_ne = std::max(max_ne, D.ne);
+    seg_cap = std::max(seg_cap, D.seg_cap);
+  }
+  int s;
+  fnum::PWBatchDev& dev = G.dev;
+  dev.n_frames = (int)G.frames.size();
+  dev.max_ne = max_ne;
+  dev.seg_cap = seg_cap;
+  G.grid = fnum::pw_tc_batch_grid(max_ne, G.window_id, nullptr);
+  fnum::PWDev* d_frames = nullptr;
+  float2** d_img = nullptr;
+  float** d_w = nullptr;
+  int* d_ts = nullptr;
+  std::vector<unsigned long long> zero(1, 0);
+  unsigned long long* d_counter = nullptr;
+  if ((s = batch_upload(B, &d_frames, frames)) || (s = batch_upload(B, &d_img, images)) ||
+      (s = batch_upload(B, &d_w, weights)) || (s = batch_upload(B, &d_ts, tile_start)) ||
+      (s = batch_upload(B, &d_counter, zero)))
+    return s;
+  void* seg = nullptr;
+  cudaError_t e = cudaMalloc(&seg, (size_t)G.grid * fnum::NTHREADS * seg_cap * fnum::PW_SEG_INT4 * sizeof(int4));
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return cuda_status(e);
+  }
+  B->allocs.push_back(seg);
+  dev.frames = d_frames;
+  dev.images = d_img;
+  dev.weights = d_w;
+  dev.tile_start = d_ts;
+  dev.counter = d_counter;
+  dev.seg = (int4*)seg;
+  return FNUM_OK;
+}
+
+}  // namespace
+}  // extern "C++"
 
 int fnum_batch_create(fnum_plan* const* plans, int n, const void* const* d_rf, const int* rf_is_double,
                       void* const* d_images, float* const* d_weights, float* const* d_weights_rx, int n_streams,
@@ -1425,12 +1570,6 @@ int fnum_batch_create(fnum_plan* const* plans, int n, const void* const* d_rf, c
   for (int i = 0; i < n; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int b) { return plans[a]->info.terms > plans[b]->info.terms; });
-  std::vector<double> load(k, 0.0);
-  for (int f : order) {
-    const int b = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-    branch[f] = b;
-    load[b] += (double)plans[f]->info.terms;
-  }
   fnum_batch* B = new (std::nothrow) fnum_batch;
   if (!B) return FNUM_ERR_ARGUMENT;
   B->device = plans[0]->device;
@@ -1444,14 +1583,72 @@ int fnum_batch_create(fnum_plan* const* plans, int n, const void* const* d_rf, c
   for (int i = 0; i < n && e == cudaSuccess; ++i) e = cudaEventCreate(&B->done[i]);
   for (int i = 0; i < k && e == cudaSuccess; ++i) e = cudaStreamCreateWithFlags(&st[i], cudaStreamNonBlocking);
   for (int i = 0; i < k && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&fj[i], cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaStreamBeginCapture(st[0], cudaStreamCaptureModeThreadLocal);
-  capturing = (e == cudaSuccess);
-  if (e == cudaSuccess) e = cudaEventRecordWithFlags(B->start, st[0], cudaEventRecordExternal);
-  if (e == cudaSuccess) e = cudaEventRecord(fj[0], st[0]);
-  for (int i = 1; i < k && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(st[i], fj[0], 0);
-  if (e != cudaSuccess) s = cuda_status(e);
+  // compounded tensor-core frames go to persistent launches (one per window), the others
+  // keep a launch per frame on the branches
+  std::vector<char> persistent(n, 0);
+  for (int f : order) {
+    if (!tc_persistent(plans[f])) continue;
+    persistent[f] = 1;
+    const int w = plans[f]->pw.window_id;
+    size_t gi = 0;
+    while (gi < B->groups.size() && B->groups[gi].window_id != w) ++gi;
+    if (gi == B->groups.size()) {
+      B->groups.emplace_back();
+      B->groups.back().window_id = w;
+    }
+    B->groups[gi].frames.push_back(f);   // `order` is largest first
+    ++B->persistent_frames;
+  }
+  for (auto& G : B->groups)
+    if ((s = build_tc_group(B, G, plans, d_images, d_weights))) break;
+  // the other frames: each to the least-loaded branch (not branch 0, which runs the
+  // persistent launches, when there are other branches)
+  {
+    const int b0 = (k > 1 && B->persistent_frames > 0) ? 1 : 0;
+    std::vector<double> load(k, 0.0);
+    for (int f : order) {
+      if (persistent[f]) continue;
+      const int b = (int)(std::min_element(load.begin() + b0, load.end()) - load.begin());
+      branch[f] = b;
+      load[b] += (double)plans[f]->info.terms;
+    }
+  }
+  std::vector<cudaEvent_t> prep(k, nullptr);   // the persistent frames' DFTs done, per branch
+  for (int i = 0; i < k && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&prep[i], cudaEventDisableTiming);
+  if (e == cudaSuccess && !s) e = cudaStreamBeginCapture(st[0], cudaStreamCaptureModeThreadLocal);
+  capturing = (e == cudaSuccess && !s);
+  if (e == cudaSuccess && !s) e = cudaEventRecordWithFlags(B->start, st[0], cudaEventRecordExternal);
+  if (e == cudaSuccess && !s) e = cudaEventRecord(fj[0], st[0]);
+  for (int i = 1; i < k && e == cudaSuccess && !s; ++i) e = cudaStreamWaitEvent(st[i], fj[0], 0);
+  if (e != cudaSuccess && !s) s = cuda_status(e);
+  // the persistent frames' band DFTs, spectra fragments and counters, spread over the
+  // branches; then branch 0 waits for them all and runs the persistent launches
+  if (B->persistent_frames > 0) {
+    int rr = 0;
+    for (int f : order) {
+      if (s || !persistent[f]) continue;
+      cudaStream_t q = st[rr++ % k];
+      if ((s = plan_dft(plans[f], d_rf[f], rf_is_double ? rf_is_double[f] : 0, q))) break;
+      e = cudaMemsetAsync(plans[f]->counters, 0, 5 * sizeof(unsigned long long), q);
+      if (e == cudaSuccess) e = fnum::launch_pw_tc_prep(plans[f]->pw, q);
+      if (e != cudaSuccess) s = cuda_status(e);
+    }
+    for (int i = 1; i < k && !s; ++i) {
+      e = cudaEventRecord(prep[i], st[i]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st[0], prep[i], 0);
+      if (e != cudaSuccess) s = cuda_status(e);
+    }
+    for (auto& G : B->groups) {
+      if (s) break;
+      e = fnum::launch_pw_tc_batch(G.dev, G.window_id, G.grid, st[0]);
+      for (size_t j = 0; j < G.frames.size() && e == cudaSuccess; ++j)
+        e = cudaEventRecordWithFlags(B->done[G.frames[j]], st[0], cudaEventRecordExternal);
+      if (e != cudaSuccess) s = cuda_status(e);
+    }
+  }
   for (int f : order) {
     if (s) break;
+    if (persistent[f]) continue;
     cudaStream_t q = st[branch[f]];
     if ((s = plan_dft(plans[f], d_rf[f], rf_is_double ? rf_is_double[f] : 0, q))) break;
     if ((s = plan_beamform(plans[f], d_images[f], d_weights ? d_weights[f] : nullptr,
@@ -1479,6 +1676,7 @@ int fnum_batch_create(fnum_plan* const* plans, int n, const void* const* d_rf, c
   }
   for (int i = 0; i < k; ++i) {
     if (fj[i]) cudaEventDestroy(fj[i]);
+    if (prep[i]) cudaEventDestroy(prep[i]);
     if (st[i]) cudaStreamDestroy(st[i]);
   }
   (void)cudaGetLastError();
@@ -1507,6 +1705,13 @@ int fnum_batch_frame_times(const fnum_batch* batch, float* ms) {
       return cuda_status(e);
     }
   }
+  return FNUM_OK;
+}
+
+int fnum_batch_info(const fnum_batch* batch, int* persistent_frames, int* persistent_launches) {
+  if (!batch) return FNUM_ERR_ARGUMENT;
+  if (persistent_frames) *persistent_frames = batch->persistent_frames;
+  if (persistent_launches) *persistent_launches = (int)batch->groups.size();
   return FNUM_OK;
 }
 

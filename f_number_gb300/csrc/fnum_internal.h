@@ -42,6 +42,10 @@ struct PWDev {
   int flush_chunks;    // flush Horner accumulators every flush_chunks * KCHUNK bins
   float scale;         // 2 / N_dft
   int variant;         // fused kernel variant, 0 = by angle count (launch_pw_fused)
+  // launch shape picked by the autotuner (0 = default): resident blocks per SM, and the
+  // bins between exact re-anchorings of the tensor-core kernel (32 or 16)
+  int blocks_per_sm;
+  int tc_tb;
   // per column [nx]
   const dfl* col_u;    // K_u x
   const dfl* col_p;    // M + x / pitch
@@ -114,6 +118,20 @@ struct SADev {
   float M_f, pitch_f, coef_f, add_f;
 };
 
+// One persistent launch of the tensor-core beamformer over the tiles of many
+// compounded frames (fnum_batch_*): per-frame descriptors and outputs in device
+// memory, the tiles numbered frame after frame (tile_start holds the prefix sums),
+// one tile counter and one segment scratch for the launch.
+struct PWBatchDev {
+  const PWDev* frames;       // [n_frames]
+  float2* const* images;     // [n_frames] image of each frame
+  float* const* weights;     // [n_frames] weights of each frame (entries may be null)
+  const int* tile_start;     // [n_frames + 1]
+  int n_frames, max_ne, seg_cap;
+  unsigned long long* counter;
+  int4* seg;                 // [grid][NTHREADS][seg_cap]
+};
+
 // error bits in counters[2] (beamformers) and counters[5] (band DFT)
 constexpr unsigned long long ERR_SEG_OVERFLOW = 1ull;
 constexpr unsigned long long ERR_DFT_TIMEOUT = 2ull;   // a wait of the tensor-core DFT gave up
@@ -153,6 +171,12 @@ int pw_variant_count();
 int pw_variant_of(const PWDev& d);
 int sa_fused_grid(const SADev& d, int* blocks_per_sm);
 cudaError_t launch_pw_fused(const PWDev& d, int grid, float2* image, float* weights, cudaStream_t s);
+// the tensor-core variant's spectra scale and B fragments for frame d (before a batch launch)
+cudaError_t launch_pw_tc_prep(const PWDev& d, cudaStream_t s);
+// tiles of a frame for the tensor-core kernel; grid of the batch kernel with all blocks resident
+int pw_tc_tiles(const PWDev& d);
+int pw_tc_batch_grid(int max_ne, int window_id, int* blocks_per_sm);
+cudaError_t launch_pw_tc_batch(const PWBatchDev& B, int window_id, int grid, cudaStream_t s);
 cudaError_t launch_pw_plain(const PWDev& d, float2* image, float* weights, cudaStream_t s);
 constexpr int M_MAXE = 256;   // elements supported by the das_pw.m-semantics kernel
 cudaError_t launch_pw_m(const PWDev& d, int compound, float2* image, float* weights, cudaStream_t s);

@@ -1026,7 +1026,7 @@ pw_event_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ w
 // aperture data (inverse half-widths, 1/W) come from the segment lists through a
 // table in shared memory that lanes 0..15 of each warp fill ahead of the bins.
 constexpr int TC_WARPS = NTHREADS / 32;
-constexpr int TC_TB = 32;   // bins per flush and receive-phasor re-anchoring
+constexpr int TC_TB = 32;   // bins per flush and receive-phasor re-anchoring (at most; PWDev::tc_tb may pick 16)
 constexpr int TC_TT = 16;   // bins per aperture table
 
 __device__ __forceinline__ void tc_split(float x0, float x1, unsigned& hi, unsigned& lo) {
@@ -1103,50 +1103,48 @@ __global__ void __launch_bounds__(256) tc_prep_kernel(const PWDev d, int n_ap) {
   d.tc_B[i] = o;
 }
 
-template <int WIN>
-__global__ void __launch_bounds__(NTHREADS, 4)
-pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weights, int n_tiles_x, int n_tiles_z) {
-  __shared__ float4 apt[TC_WARPS][TC_TT][16];   // {-, 1/L_left, 1/L_right, 1/W} per bin, voxel
-  __shared__ int e_range[2];
-  __shared__ int s_tile;
-  __shared__ int s_nseg[TC_WARPS * 16];
+// Shared memory of pw_tc_kernel's tile body.
+struct TcShared {
+  float4 apt[TC_WARPS][TC_TT][16];   // {-, 1/L_left, 1/L_right, 1/W} per bin, voxel
+  int e_range[2];
+  int s_nseg[TC_WARPS * 16];
   // table builders' state (entry in effect, next segment entry, its index) and the
   // threads' compensated sums per voxel, kept out of registers
-  __shared__ float4 b_ent[TC_WARPS * 16];
-  __shared__ int4 b_next[TC_WARPS * 16];
-  __shared__ int b_idx[TC_WARPS * 16];
-  __shared__ float4 s_acc[2][NTHREADS];   // {acc.x, acc.y, comp.x, comp.y} per voxel V
+  float4 b_ent[TC_WARPS * 16];
+  int4 b_next[TC_WARPS * 16];
+  int b_idx[TC_WARPS * 16];
+  float4 s_acc[2][NTHREADS];   // {acc.x, acc.y, comp.x, comp.y} per voxel V
   // conj(r) of the thread's (voxel, element) pairs, packed over the two elements i of a
   // (voxel, k-step): {re, re}, {im, im}, {-im, -im}
-  __shared__ float2 s_cr[2 * TC_KS][3][NTHREADS];
-  __shared__ float2 s_dx[4 * TC_KS][NTHREADS];   // |c_e - x| of the pairs as {left side, right side}, the other 0
-  extern __shared__ __align__(16) unsigned char dyn[];  // lb[ne], ub[ne] (dfl), ktop[ne]
-  dfl* lb_s = (dfl*)dyn;
-  dfl* ub_s = lb_s + d.ne;
-  int* ktop = (int*)(ub_s + d.ne);
+  float2 s_cr[2 * TC_KS][3][NTHREADS];
+  float2 s_dx[4 * TC_KS][NTHREADS];   // |c_e - x| of the pairs as {left side, right side}, the other 0
+};
 
+// One 64-voxel tile of frame d (2 columns x 32 rows): segment lists, then the bin loop
+// on the tensor cores, then the image.  The caller has reset ktop[] and e_range and
+// synchronised the block; the body ends with a block barrier.  lb_s / ub_s hold the
+// frame's element edges.
+template <int WIN>
+__device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles_x, int n_tiles_z, TcShared& sh,
+                                           const dfl* lb_s, const dfl* ub_s, int* ktop, float2* __restrict__ image,
+                                           float* __restrict__ weights, unsigned long long& n_active,
+                                           unsigned long long& n_empty, unsigned long long& n_exec) {
+  auto& apt = sh.apt;
+  auto& e_range = sh.e_range;
+  auto& s_nseg = sh.s_nseg;
+  auto& b_ent = sh.b_ent;
+  auto& b_next = sh.b_next;
+  auto& b_idx = sh.b_idx;
+  auto& s_acc = sh.s_acc;
+  auto& s_cr = sh.s_cr;
+  auto& s_dx = sh.s_dx;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int g = lane >> 2, q = lane & 3;
-  const int n_tiles = n_tiles_x * n_tiles_z;
   int4* seg_blk = d.seg + (size_t)blockIdx.x * NTHREADS * (size_t)d.seg_cap * PW_SEG_INT4;
   const float inv_par = (d.window_par > 0.0f) ? 1.0f / d.window_par : 0.0f;
   const float inv_sigma = 1.0f / tc_scale(*d.tc_max);
-  unsigned long long n_active = 0, n_empty = 0, n_exec = 0;
-  for (int e = tid; e < d.ne; e += NTHREADS) {
-    lb_s[e] = d.el_lb[e];
-    ub_s[e] = d.el_ub[e];
-  }
-
-  for (;;) {
-    if (tid == 0) s_tile = (int)atomicAdd(&d.counters[3], 1ull);
-    for (int e = tid; e < d.ne; e += NTHREADS) ktop[e] = -1;
-    if (tid == 0) {
-      e_range[0] = d.ne;
-      e_range[1] = -1;
-    }
-    __syncthreads();
-    const int tile = s_tile;
-    if (tile >= n_tiles) break;
+  const int tb = (d.tc_tb > 0 && d.tc_tb < TC_TB) ? d.tc_tb : TC_TB;   // bins per flush (a launch shape)
+  {
     int tx, tz;
     tile_coords(tile, n_tiles_x, n_tiles_z, tx, tz);
     // block voxel vb (0..63): column vb / 32, row vb % 32; threads 0..63 build its segment list
@@ -1258,8 +1256,8 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
           b_idx[bv] = bs;
         }
         const uint4* Bpe = Bp + (size_t)(e0 >> 3) * 96 + lane;
-        for (int kc_hi = kt; kc_hi >= d.k_lb; kc_hi -= TC_TB) {
-          const int kc_lo = max(d.k_lb, kc_hi - (TC_TB - 1));
+        for (int kc_hi = kt; kc_hi >= d.k_lb; kc_hi -= tb) {
+          const int kc_lo = max(d.k_lb, kc_hi - (tb - 1));
           // receive phasors re-anchored exactly at the chunk's first bin
 #pragma unroll
           for (int V = 0; V < 2; ++V) {
@@ -1396,11 +1394,109 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
     }
     __syncthreads();
   }
-  n_active *= (unsigned long long)d.na;
-  n_empty *= (unsigned long long)d.na;
-  atomicAdd(&d.counters[0], n_active);
-  atomicAdd(&d.counters[1], n_empty);
-  if (tid == 0) atomicAdd(&d.counters[4], n_exec);
+}
+
+// the per-frame statistics of pw_tc_tile, added to the frame's counters
+__device__ __forceinline__ void pw_tc_flush_counts(const PWDev& d, unsigned long long& n_active,
+                                                   unsigned long long& n_empty, unsigned long long& n_exec) {
+  atomicAdd(&d.counters[0], n_active * (unsigned long long)d.na);
+  atomicAdd(&d.counters[1], n_empty * (unsigned long long)d.na);
+  if (threadIdx.x == 0) atomicAdd(&d.counters[4], n_exec);
+  n_active = n_empty = n_exec = 0;
+}
+
+template <int WIN>
+__global__ void __launch_bounds__(NTHREADS, 4)
+pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weights, int n_tiles_x, int n_tiles_z) {
+  __shared__ TcShared sh;
+  __shared__ int s_tile;
+  extern __shared__ __align__(16) unsigned char dyn[];  // lb[ne], ub[ne] (dfl), ktop[ne]
+  dfl* lb_s = (dfl*)dyn;
+  dfl* ub_s = lb_s + d.ne;
+  int* ktop = (int*)(ub_s + d.ne);
+  const int tid = threadIdx.x;
+  const int n_tiles = n_tiles_x * n_tiles_z;
+  unsigned long long n_active = 0, n_empty = 0, n_exec = 0;
+  for (int e = tid; e < d.ne; e += NTHREADS) {
+    lb_s[e] = d.el_lb[e];
+    ub_s[e] = d.el_ub[e];
+  }
+  for (;;) {
+    if (tid == 0) s_tile = (int)atomicAdd(&d.counters[3], 1ull);
+    for (int e = tid; e < d.ne; e += NTHREADS) ktop[e] = -1;
+    if (tid == 0) {
+      sh.e_range[0] = d.ne;
+      sh.e_range[1] = -1;
+    }
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= n_tiles) break;
+    pw_tc_tile<WIN>(d, tile, n_tiles_x, n_tiles_z, sh, lb_s, ub_s, ktop, image, weights, n_active, n_empty, n_exec);
+  }
+  pw_tc_flush_counts(d, n_active, n_empty, n_exec);
+}
+
+// One persistent launch over the tiles of many frames (a batch): each block draws
+// global tile numbers from the batch's counter, in frame order (the host orders the
+// frames largest first), finds the tile's frame, and runs pw_tc_tile on it with the
+// frame's descriptor copied to shared memory and the batch's segment scratch.
+template <int WIN>
+__global__ void __launch_bounds__(NTHREADS, 4) pw_tc_batch_kernel(const PWBatchDev B) {
+  __shared__ TcShared sh;
+  __shared__ PWDev sd;
+  __shared__ int s_tile, s_frame;
+  extern __shared__ __align__(16) unsigned char dyn[];  // lb[max_ne], ub[max_ne] (dfl), ktop[max_ne]
+  dfl* lb_s = (dfl*)dyn;
+  dfl* ub_s = lb_s + B.max_ne;
+  int* ktop = (int*)(ub_s + B.max_ne);
+  const int tid = threadIdx.x;
+  unsigned long long n_active = 0, n_empty = 0, n_exec = 0;
+  int cur = -1;
+  for (;;) {
+    if (tid == 0) {
+      const int t = (int)atomicAdd(B.counter, 1ull);
+      int f = -1;
+      if (t < B.tile_start[B.n_frames]) {
+        int lo = 0, hi = B.n_frames - 1;   // the frame whose tile range holds t
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (B.tile_start[mid] <= t) lo = mid; else hi = mid - 1;
+        }
+        f = lo;
+        s_tile = t - B.tile_start[f];
+      }
+      s_frame = f;
+    }
+    __syncthreads();
+    const int f = s_frame;
+    if (f < 0) break;
+    if (f != cur) {
+      if (cur >= 0) pw_tc_flush_counts(sd, n_active, n_empty, n_exec);
+      __syncthreads();   // every thread is done with the previous frame's descriptor
+      const int* src = reinterpret_cast<const int*>(B.frames + f);
+      int* dst = reinterpret_cast<int*>(&sd);
+      for (int w = tid; w < (int)(sizeof(PWDev) / sizeof(int)); w += NTHREADS) dst[w] = src[w];
+      __syncthreads();
+      if (tid == 0) {
+        sd.seg = B.seg;
+        sd.seg_cap = B.seg_cap;
+      }
+      for (int e = tid; e < sd.ne; e += NTHREADS) {
+        lb_s[e] = sd.el_lb[e];
+        ub_s[e] = sd.el_ub[e];
+      }
+      cur = f;
+    }
+    for (int e = tid; e < B.max_ne; e += NTHREADS) ktop[e] = -1;
+    if (tid == 0) {
+      sh.e_range[0] = sd.ne;
+      sh.e_range[1] = -1;
+    }
+    __syncthreads();
+    const int ntx = (sd.nx + TC_TILE_X - 1) / TC_TILE_X, ntz = (sd.nz + TILE_Z - 1) / TILE_Z;
+    pw_tc_tile<WIN>(sd, s_tile, ntx, ntz, sh, lb_s, ub_s, ktop, B.images[f], B.weights[f], n_active, n_empty, n_exec);
+  }
+  if (cur >= 0) pw_tc_flush_counts(sd, n_active, n_empty, n_exec);
 }
 
 typedef void (*pw_kernel_t)(const PWDev, float2*, float*, int, int);
@@ -1482,6 +1578,7 @@ int pw_fused_grid(const PWDev& d, int* blocks_per_sm) {
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, NTHREADS, (size_t)d.ne * (sizeof(int) + 2 * sizeof(dfl)));
   if (bps < 1) bps = 1;
+  if (d.blocks_per_sm > 0 && d.blocks_per_sm < bps) bps = d.blocks_per_sm;   // a launch shape of the autotuner
   if (blocks_per_sm) *blocks_per_sm = bps;
   const int tiles = pw_tiles_x(d) * ((d.nz + TILE_Z - 1) / TILE_Z);
   return tiles < nsm * bps ? tiles : nsm * bps;
@@ -1492,6 +1589,7 @@ int pw_fused_max_grid(const PWDev& d) {
   for (int v = 1; v <= pw_variant_count(); ++v) {
     PWDev t = d;
     t.variant = v;
+    t.blocks_per_sm = 0;
     g = max(g, pw_fused_grid(t, nullptr));
   }
   return g;
@@ -1503,17 +1601,51 @@ cudaError_t launch_pw_fused(const PWDev& d, int grid, float2* image, float* weig
   // each launch draws tiles from a fresh counter
   cudaError_t e = cudaMemsetAsync(d.counters + 3, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
-  if (pw_variant_of(d) == TC_VARIANT) {
-    if (!d.tc_B || !d.tc_max) return cudaErrorInvalidValue;
-    // spectra -> fp16 B fragments, scaled by a power of two set by their largest component
-    e = cudaMemsetAsync(d.tc_max, 0, sizeof(unsigned), s);
-    if (e != cudaSuccess) return e;
-    tc_absmax_kernel<<<304, 256, 0, s>>>(d, d.tc_max);
-    const int n_ap = (d.na + TC_NA - 1) / TC_NA;
-    const size_t n = (size_t)n_ap * d.K * d.tc_S * 96;
-    tc_prep_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, n_ap);
-  }
+  if (pw_variant_of(d) == TC_VARIANT && (e = launch_pw_tc_prep(d, s)) != cudaSuccess) return e;
   pw_pick(d)<<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, ntz);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pw_tc_prep(const PWDev& d, cudaStream_t s) {
+  if (!d.tc_B || !d.tc_max) return cudaErrorInvalidValue;
+  // spectra -> fp16 B fragments, scaled by a power of two set by their largest component
+  cudaError_t e = cudaMemsetAsync(d.tc_max, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
+  tc_absmax_kernel<<<304, 256, 0, s>>>(d, d.tc_max);
+  const int n_ap = (d.na + TC_NA - 1) / TC_NA;
+  const size_t n = (size_t)n_ap * d.K * d.tc_S * 96;
+  tc_prep_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, n_ap);
+  return cudaGetLastError();
+}
+
+int pw_tc_tiles(const PWDev& d) { return ((d.nx + TC_TILE_X - 1) / TC_TILE_X) * ((d.nz + TILE_Z - 1) / TILE_Z); }
+
+typedef void (*pw_tc_batch_t)(const PWBatchDev);
+static pw_tc_batch_t pw_tc_batch_pick(int window_id) {
+  switch (window_id) {
+    case 0: return pw_tc_batch_kernel<0>;
+    case 1: return pw_tc_batch_kernel<1>;
+    case 2: return pw_tc_batch_kernel<2>;
+    default: return pw_tc_batch_kernel<4>;
+  }
+}
+
+int pw_tc_batch_grid(int max_ne, int window_id, int* blocks_per_sm) {
+  int dev = 0, nsm = 0, bps = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pw_tc_batch_pick(window_id), NTHREADS,
+                                                (size_t)max_ne * (sizeof(int) + 2 * sizeof(dfl)));
+  if (bps < 1) bps = 1;
+  if (blocks_per_sm) *blocks_per_sm = bps;
+  return nsm * bps;
+}
+
+cudaError_t launch_pw_tc_batch(const PWBatchDev& B, int window_id, int grid, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(B.counter, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  const size_t smem = (size_t)B.max_ne * (sizeof(int) + 2 * sizeof(dfl));
+  pw_tc_batch_pick(window_id)<<<grid, NTHREADS, smem, s>>>(B);
   return cudaGetLastError();
 }
 // ---------------------------------------------------------------------------

@@ -499,6 +499,10 @@ class _Plan:
                                                  _lib.C.byref(v), _lib.C.byref(ms)), self._saft)
         return v.value, ms.value
 
+    def set_shape(self, blocks_per_sm=0, bin_chunk=0):
+        """Pins the launch shape of the current variant (fnum_plan_set_shape)."""
+        _lib.check(_lib.lib().fnum_plan_set_shape(self._ptr, int(blocks_per_sm), int(bin_chunk)), self._saft)
+
     def set_kernel_variant(self, variant):
         """Pins the fused kernel's variant (fnum_plan_set_kernel_variant): 0 = by the
         angle count, 1..9 for a plane-wave plan."""
@@ -712,6 +716,12 @@ class Batch:
 
     def execute(self, stream=None):
         _lib.check(_lib.lib().fnum_batch_execute(self._ptr, _Plan._stream_ptr(stream)))
+
+    def persistent(self):
+        """(frames carried by persistent tensor-core launches, number of such launches)."""
+        f, l = _lib.C.c_int(0), _lib.C.c_int(0)
+        _lib.check(_lib.lib().fnum_batch_info(self._ptr, _lib.C.byref(f), _lib.C.byref(l)))
+        return f.value, l.value
 
     def frame_times(self):
         """Completion time of each frame in ms from the start of the last execute."""

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define FNUM_ABI_VERSION 3
+#define FNUM_ABI_VERSION 4
 
 typedef enum fnum_status {
   FNUM_OK = 0,
@@ -209,6 +209,9 @@ typedef struct fnum_plan_info {
   long long executed_terms;        /* recurrence steps the fused kernel ran (>= active_terms), last execute */
   int kernel_variant;              /* PW fused kernel variant (1..9, see fnum_plan_autotune); 0 for SA */
   int grid;                        /* blocks of the fused kernel's launch */
+  int blocks_per_sm;               /* PW: resident blocks per SM of that launch (launch shape) */
+  int bin_chunk;                   /* PW: bins between exact phase re-anchorings (tensor cores 32 or 16;
+                                      FP32 kernels 256 or 128) */
 } fnum_plan_info;
 
 int fnum_pw_plan_create(const fnum_pw_desc* desc, const double* steering_angles, int n_angles,
@@ -285,6 +288,15 @@ int fnum_plan_autotune(fnum_plan* plan, const void* d_rf, int rf_is_double, int*
    rounding of the per-pass sums.  A synthetic-aperture plan or a plan with
    FNUM_FLAG_M_SEMANTICS accepts only 0. */
 int fnum_plan_set_kernel_variant(fnum_plan* plan, int variant);
+/* fnum_plan_set_shape: pins the launch shape of a plane-wave plan's current
+   variant: blocks_per_sm (0 = as many as fit) and bin_chunk, the bins between
+   exact re-anchorings of the phase recurrences (0 = default; tensor cores 16 or
+   32, FP32 kernels 128 or 256).  fnum_plan_autotune, after picking the variant,
+   times these shapes (all or one fewer resident blocks, the default or the
+   shorter bin chunk) and keeps the fastest.  A shorter chunk re-anchors more
+   often, so no shape is less accurate than the default.  No counterpart in the
+   reference. */
+int fnum_plan_set_shape(fnum_plan* plan, int blocks_per_sm, int bin_chunk);
 
 /* A batch binds n frames -- distinct plans with their device RF, image and
    weight buffers -- and captures their band DFTs and beamformers into one CUDA
@@ -295,12 +307,21 @@ int fnum_plan_set_kernel_variant(fnum_plan* plan, int variant);
    graph on `stream`; fnum_batch_frame_times gives, after it completed, each
    frame's completion time in ms from the batch's start (n values, in the
    order of `plans`). */
+/* Compounded frames whose plans use the tensor-core kernel (variant 9) are not
+   launched per frame: their band DFTs and spectra fragments run on the branches,
+   then ONE persistent launch per window type beamforms all of them -- each block
+   draws tiles of all those frames from one counter, largest frames first, with
+   each frame's descriptor read from device memory -- so no SM idles between
+   frames.  The other frames keep a launch per frame on the other branches.
+   fnum_batch_info reports how many frames the persistent launches carry and how
+   many launches there are. */
 typedef struct fnum_batch fnum_batch;
 int fnum_batch_create(fnum_plan* const* plans, int n, const void* const* d_rf, const int* rf_is_double,
                       void* const* d_images, float* const* d_weights, float* const* d_weights_rx, int n_streams,
                       fnum_batch** batch);
 int fnum_batch_execute(fnum_batch* batch, void* stream);
 int fnum_batch_frame_times(const fnum_batch* batch, float* ms);
+int fnum_batch_info(const fnum_batch* batch, int* persistent_frames, int* persistent_launches);
 int fnum_batch_destroy(fnum_batch* batch);
 
 /* After an execute of a plan with FNUM_FLAG_M_SEMANTICS: the focused spectrum of

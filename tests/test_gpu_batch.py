@@ -51,6 +51,9 @@ def test_batch_equals_standalone_plans(gpu):
     images = [torch.full_like(e, float("nan")) for e in expect]
     weights = [torch.full_like(w, float("nan")) if i % 2 == 0 else None for i, w in enumerate(expect_w)]
     batch = das.Batch(plans, rfs, images, weights=weights, n_streams=3)
+    # the compounded frames with 3+ angles (tensor-core kernel) share one persistent launch
+    n_tc = sum(1 for p in plans if p.n_out == 1 and p.info()["kernel_variant"] == 9)
+    assert n_tc == 3 and batch.persistent() == (n_tc, 1)
     for rep in range(2):                        # the graph is relaunched: same results
         for im in images:
             im.fill_(float("nan"))
@@ -180,4 +183,31 @@ def test_tensor_core_variant_per_angle_images(gpu):
         o = O.das_pw_mex(px, pz, rf_np[a].T.astype(np.float64), 20e6, angles[a], arr.width, arr.pitch, 1540.0,
                          (2e6, 7e6), 0.0, windows.hann().spec(), fn.spec(), "on")[0]
         assert np.linalg.norm(img[a].T - o) / np.linalg.norm(o) < 1e-4, a
+    plan.close()
+
+
+@pytest.mark.parametrize("na", [1, 11])
+def test_launch_shapes_keep_results(gpu, na):
+    """The launch shapes the autotuner searches (fewer resident blocks, shorter bin
+    chunk between exact re-anchorings) change only scheduling and how often the
+    phase recurrences are re-anchored: images stay within 1e-5 of the default
+    shape's and within the parity bar of the FP64 oracle."""
+    rng = np.random.default_rng(31 + na)
+    plan, rf, (arr, px, pz, angles) = _frame(rng, 48, na, 1024, 32, True, gpu)
+    ref = plan.execute(rf).cpu().numpy()
+    inf = plan.info()
+    tc = inf["kernel_variant"] == 9
+    assert inf["bin_chunk"] == (32 if tc else 256)
+    rf_np = rf.cpu().numpy().astype(np.float64)
+    o = sum(O.das_pw_mex(px, pz, rf_np[a].T, 20e6, angles[a], arr.width, arr.pitch, 1540.0, (2e6, 7e6), 0.0,
+                         ("hann", 0.0), FN.spec(), "on")[0] for a in range(na))
+    for bps, chunk in [(0, 16 if tc else 128), (max(1, inf["blocks_per_sm"] - 1), 0)]:
+        plan.set_shape(bps, chunk)
+        if chunk:
+            assert plan.info()["bin_chunk"] == chunk
+        img = plan.execute(rf).cpu().numpy()
+        assert np.linalg.norm(img - ref) / np.linalg.norm(ref) < 1e-5, (bps, chunk)
+        assert np.linalg.norm(img[0].T - o) / np.linalg.norm(o) < 1e-4
+    with pytest.raises(_lib.FNumError):
+        plan.set_shape(0, 24)
     plan.close()
