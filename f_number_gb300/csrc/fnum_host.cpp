@@ -450,10 +450,11 @@ struct fnum_plan {
   float2* adj_img = nullptr;
   float2* adj_G = nullptr;     // cotangent dL/dI* of the sharpness loss
   float* adj_invw = nullptr;
-  float2* adj_H = nullptr;
+  float2* adj_D = nullptr;     // Draw of the derivative forward (dI/dc = -(2 pi i / c) Draw)
   float2* adj_gX = nullptr;
   double* adj_sums = nullptr;
-  double* adj_acc = nullptr;   // FP64 sums of the voxel slices, 4 per spectrum entry
+  double* adj_acc = nullptr;   // FP64 sums of the voxel slices, 2 per spectrum entry
+  unsigned* adj_gmax = nullptr;  // fp16 scale inputs of the adjoint: max |G|, max 1/W
   bool adj_invw_ready = false;
   // band DFT on the tensor cores: fp16 hi/lo operand planes, per-line scales, TMA maps
   fnum::DftTc dft{};
@@ -654,6 +655,7 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
   D.seg_cap = (mono ? std::min(b.K, 2 * ne + 16) : b.K) + 1;  // + the sentinel entry
   D.flush_chunks = 4;
   D.scale = (float)(2.0 / b.N);
+  D.t0N = (float)(d->index_t0 / b.N);
   D.x_na = na;
   D.x_a0 = 0;
   std::vector<dfl> ax, az, gg;
@@ -1540,6 +1542,12 @@ int build_tc_group(fnum_batch* B, fnum_batch::TcGroup& G, fnum_plan* const* plan
     return cuda_status(e);
   }
   B->allocs.push_back(seg);
+  // the descriptors the kernel reads carry the batch's segment scratch
+  for (auto& D : frames) {
+    D.seg = (int4*)seg;
+    D.seg_cap = seg_cap;
+  }
+  FNUM_CUDA(cudaMemcpy(d_frames, frames.data(), frames.size() * sizeof(fnum::PWDev), cudaMemcpyHostToDevice));
   dev.frames = d_frames;
   dev.images = d_img;
   dev.weights = d_w;
@@ -1757,26 +1765,31 @@ int adjoint_buffers(fnum_plan* plan, cudaStream_t st) {
   int s = FNUM_OK;
   if (!plan->adj_img) {
     if ((s = plan->alloc(&plan->adj_img, (size_t)nvox)) || (s = plan->alloc(&plan->adj_G, (size_t)nvox)) ||
-        (s = plan->alloc(&plan->adj_invw, (size_t)nvox * D.K)) || (s = plan->alloc(&plan->adj_H, nspec)) ||
+        (s = plan->alloc(&plan->adj_invw, (size_t)nvox * D.K)) || (s = plan->alloc(&plan->adj_D, (size_t)nvox)) ||
         (s = plan->alloc(&plan->adj_gX, nspec)) || (s = plan->alloc(&plan->adj_sums, 4)) ||
-        (s = plan->alloc(&plan->adj_acc, 4 * nspec)))
+        (s = plan->alloc(&plan->adj_acc, 2 * nspec)) || (s = plan->alloc(&plan->adj_gmax, 2)))
       return s;
   }
   if (!plan->adj_invw_ready) {
     FNUM_CUDA(fnum::launch_pw_invw(D, plan->adj_invw, st));
+    FNUM_CUDA(fnum::launch_absmax(plan->adj_invw, (size_t)nvox * D.K, plan->adj_gmax + 1, st));
     plan->adj_invw_ready = true;
   }
   return FNUM_OK;
 }
 
-// dL/dX* into gX and (if dloss_dc) dL/dc for the cotangent G = dL/dI*, on the plan's spectra
-int adjoint_core(fnum_plan* plan, const float2* G, float2* gX, double* dloss_dc, cudaStream_t st) {
+// dL/dX* into gX and (if dloss_dc) dL/dc for the cotangent G = dL/dI*, on the plan's
+// spectra.  dL/dc needs the derivative image adj_D of those spectra: have_D says that the
+// caller has just computed it (launch_pw_tc_deriv), else it is computed here.
+int adjoint_core(fnum_plan* plan, const float2* G, float2* gX, double* dloss_dc, bool have_D, cudaStream_t st) {
   fnum::PWDev& D = plan->pw;
-  FNUM_CUDA(fnum::launch_pw_adjoint(D, G, plan->adj_invw, (float)(plan->t0 / plan->band.N), gX, plan->adj_H,
-                                    plan->adj_acc, st));
+  const long long nvox = (long long)D.nx * D.nz;
   if (dloss_dc) {
-    const double coef = 4.0 * M_PI * (2.0 / plan->band.N) / plan->c;
-    FNUM_CUDA(fnum::launch_pw_dldc(D, plan->adj_H, coef, plan->adj_sums + 2, st));
+    if (!have_D) FNUM_CUDA(fnum::launch_pw_tc_deriv(D, plan->adj_img, plan->adj_D, st));
+    FNUM_CUDA(fnum::launch_pw_dc_reduce(G, plan->adj_D, nvox, 4.0 * M_PI / plan->c, plan->adj_sums + 2, st));
+  }
+  if (gX) FNUM_CUDA(fnum::launch_pw_adjoint(D, G, plan->adj_invw, plan->adj_gmax, gX, plan->adj_acc, st));
+  if (dloss_dc) {
     double g = 0.0;
     FNUM_CUDA(cudaMemcpyAsync(&g, plan->adj_sums + 2, sizeof(double), cudaMemcpyDeviceToHost, st));
     FNUM_CUDA(cudaStreamSynchronize(st));
@@ -1805,7 +1818,7 @@ int fnum_pw_adjoint(fnum_plan* plan, const void* d_cotangent, void* d_grad_spect
   int s;
   if ((s = fnum::adjoint_buffers(plan, st))) return s;
   float2* gX = d_grad_spectra ? (float2*)d_grad_spectra : plan->adj_gX;
-  return fnum::adjoint_core(plan, (const float2*)d_cotangent, gX, dloss_dc, st);
+  return fnum::adjoint_core(plan, (const float2*)d_cotangent, gX, dloss_dc, false, st);
 }
 
 int fnum_pw_sharpness_grad(fnum_plan* plan, const void* d_rf, int rf_is_double, double* loss, double* dloss_dc,
@@ -1819,7 +1832,8 @@ int fnum_pw_sharpness_grad(fnum_plan* plan, const void* d_rf, int rf_is_double, 
   int s = FNUM_OK;
   if ((s = fnum::adjoint_buffers(plan, st))) return s;
   if ((s = plan_dft(plan, d_rf, rf_is_double, st))) return s;
-  if ((s = plan_beamform(plan, plan->adj_img, nullptr, nullptr, st))) return s;
+  // the image and its derivative in c in one pass of the tensor-core kernel
+  FNUM_CUDA(fnum::launch_pw_tc_deriv(D, plan->adj_img, plan->adj_D, st));
   FNUM_CUDA(fnum::launch_pw_sharp_sums(plan->adj_img, nvox, plan->adj_sums, st));
   double S[2] = {0.0, 0.0};
   FNUM_CUDA(cudaMemcpyAsync(S, plan->adj_sums, sizeof(S), cudaMemcpyDeviceToHost, st));
@@ -1834,7 +1848,7 @@ int fnum_pw_sharpness_grad(fnum_plan* plan, const void* d_rf, int rf_is_double, 
   }
   const double gs2 = 1.0 / (S[0] * S[0]), gs4 = S[1] / (S[0] * S[0] * S[0]);
   FNUM_CUDA(fnum::launch_pw_sharp_cotangent(plan->adj_img, nvox, (float)gs2, (float)gs4, plan->adj_G, st));
-  if ((s = fnum::adjoint_core(plan, plan->adj_G, gX, dloss_dc, st))) return s;
+  if ((s = fnum::adjoint_core(plan, plan->adj_G, gX, dloss_dc, true, st))) return s;
   if (loss) *loss = -S[1] / (S[0] * S[0]);
   return FNUM_OK;
 }

@@ -41,6 +41,7 @@ struct PWDev {
   int seg_cap;         // segment entries per voxel
   int flush_chunks;    // flush Horner accumulators every flush_chunks * KCHUNK bins
   float scale;         // 2 / N_dft
+  float t0N;           // index_t0 / N_dft, the part of tx_ax that does not scale with 1/c
   int variant;         // fused kernel variant, 0 = by angle count (launch_pw_fused)
   // launch shape picked by the autotuner (0 = default): resident blocks per SM, and the
   // bins between exact re-anchorings of the tensor-core kernel (32 or 16)
@@ -171,6 +172,9 @@ int pw_variant_count();
 int pw_variant_of(const PWDev& d);
 int sa_fused_grid(const SADev& d, int* blocks_per_sm);
 cudaError_t launch_pw_fused(const PWDev& d, int grid, float2* image, float* weights, cudaStream_t s);
+// the compounded image and, in dimage, Draw with dI/dc = -(2 pi i / c) Draw (tensor cores;
+// prepares the fragments itself)
+cudaError_t launch_pw_tc_deriv(const PWDev& d, float2* image, float2* dimage, cudaStream_t s);
 // the tensor-core variant's spectra scale and B fragments for frame d (before a batch launch)
 cudaError_t launch_pw_tc_prep(const PWDev& d, cudaStream_t s);
 // tiles of a frame for the tensor-core kernel; grid of the batch kernel with all blocks resident
@@ -187,10 +191,15 @@ cudaError_t launch_pw_invw(const PWDev& d, float* invw, cudaStream_t s);
 cudaError_t launch_pw_sharp_sums(const float2* img, long long n, double* sums, cudaStream_t s);
 // G = dL/dI* of the sharpness loss from the image and its sums (gs2 = 1/S2^2, gs4 = S4/S2^3)
 cudaError_t launch_pw_sharp_cotangent(const float2* img, long long n, float gs2, float gs4, float2* G, cudaStream_t s);
-// adjoint of the compounded beamformer for a cotangent G = dL/dI* [nx][nz]: gX = dL/dX* and
-// H = sum_v G_v b e^{-2 pi i k u} U (for dL/dc); acc: 4 doubles per spectrum entry
-cudaError_t launch_pw_adjoint(const PWDev& d, const float2* cot, const float* invw, float t0N, float2* gX, float2* H,
+// adjoint of the compounded beamformer for a cotangent G = dL/dI* [nx][nz] on the tensor
+// cores: gX = dL/dX*; acc: 2 doubles per spectrum entry
+// gmax: two device words, [1] = max 1/W (launch_absmax over the 1/W table, once), [0] set here
+cudaError_t launch_pw_adjoint(const PWDev& d, const float2* cot, const float* invw, unsigned* gmax, float2* gX,
                               double* acc, cudaStream_t s);
-cudaError_t launch_pw_dldc(const PWDev& d, const float2* H, double coef, double* out, cudaStream_t s);
+// float bits of max |x_i| of n floats into *out
+cudaError_t launch_absmax(const float* x, size_t n, unsigned* out, cudaStream_t s);
+// dL/dc = coef sum_v Im(conj(G_v) D_v) into *out (FP64)
+cudaError_t launch_pw_dc_reduce(const float2* G, const float2* D, long long n, double coef, double* out,
+                               cudaStream_t s);
 
 }  // namespace fnum

@@ -1120,15 +1120,34 @@ struct TcShared {
   float2 s_dx[4 * TC_KS][NTHREADS];   // |c_e - x| of the pairs as {left side, right side}, the other 0
 };
 
+// Extra shared memory of the derivative variant: the pairs' receive delays and the
+// compensated sums of dI/dc per voxel.
+struct TcDerivShared {
+  float s_urx[4 * TC_KS][NTHREADS];   // u_rx of the thread's (voxel, element) pairs
+  float4 s_dacc[2][NTHREADS];
+};
+
 // One 64-voxel tile of frame d (2 columns x 32 rows): segment lists, then the bin loop
 // on the tensor cores, then the image.  The caller has reset ktop[] and e_range and
 // synchronised the block; the body ends with a block barrier.  lb_s / ub_s hold the
 // frame's element edges.
-template <int WIN>
+//
+// DERIV also writes the image's derivative with respect to the speed of sound, with
+// the band, F table and apertures held fixed (fnum_pw_sharpness_grad, fnum_pw_adjoint).
+// The phase of a term is 2 pi k u with u = U + t0/N and dU/dc = -U/c, U = u_rx + U_tx,
+// so dI/dc = -(2 pi i / c) Draw with
+//   Draw_v = s sum_k k sum_a t^k [U_tx(v,a) G_k(v,a) + G'_k(v,a)],
+//   G'_k(v,a) = sum_e (R_k(v,e) u_rx(v,e)) X_k(e,a)
+// (G' is a second product with the A operand scaled by u_rx).  sum_k k t^k Y_k comes from
+// a second Horner chain beside each first one: going down the bins, Q <- (Q + P) t
+// before P <- P t + Y, and a chunk ending at bin kc_lo contributes t^kc_lo (kc_lo P + Q).
+// dimage receives Draw (scaled like the image).
+template <int WIN, bool DERIV>
 __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles_x, int n_tiles_z, TcShared& sh,
                                            const dfl* lb_s, const dfl* ub_s, int* ktop, float2* __restrict__ image,
                                            float* __restrict__ weights, unsigned long long& n_active,
-                                           unsigned long long& n_empty, unsigned long long& n_exec) {
+                                           unsigned long long& n_empty, unsigned long long& n_exec,
+                                           TcDerivShared* dsh = nullptr, float2* __restrict__ dimage = nullptr) {
   auto& apt = sh.apt;
   auto& e_range = sh.e_range;
   auto& s_nseg = sh.s_nseg;
@@ -1199,6 +1218,7 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
       return make_float4(0.0f, il, ir, __int_as_float(c.z));
     };
     s_acc[0][tid] = s_acc[1][tid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if constexpr (DERIV) dsh->s_dacc[0][tid] = dsh->s_dacc[1][tid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 
     for (int a0 = 0; a0 < d.na; a0 += TC_NA) {
       float2 tph[2][3];   // transmit phasor of (voxel V, angle a0 + 4j + q)
@@ -1231,7 +1251,9 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
               const float dx = fabsf((cm.x - xm.x) + (cm.y - xm.y));
               const bool left = e0 + 8 * s + 2 * q + i < emid[V];
               s_dx[2 * TC_KS * V + 2 * s + i][tid] = make_float2(left ? dx : 0.0f, left ? 0.0f : dx);
-              const float2 r = cis_ku(1, df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2)));
+              const dfl urx = df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2));
+              const float2 r = cis_ku(1, urx);
+              if constexpr (DERIV) dsh->s_urx[2 * TC_KS * V + 2 * s + i][tid] = urx.x + urx.y;
               float* c = reinterpret_cast<float*>(&s_cr[TC_KS * V + s][0][tid]);
               c[i] = r.x;
               reinterpret_cast<float*>(&s_cr[TC_KS * V + s][1][tid])[i] = -r.y;
@@ -1241,6 +1263,14 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
         float H[3][4];
 #pragma unroll
         for (int j = 0; j < 3; ++j) H[j][0] = H[j][1] = H[j][2] = H[j][3] = 0.0f;
+        // derivative chains: HQ (second chain of H), HP (the u_rx-scaled product), HPQ
+        float HQ[3][4], HP[3][4], HPQ[3][4];
+        if constexpr (DERIV) {
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) HQ[j][c] = HP[j][c] = HPQ[j][c] = 0.0f;
+        }
         // builder state: the segment in effect and the next entry
         if (lane < 16) {
           int bs = 0;
@@ -1301,13 +1331,24 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
               float4 en[2];
               en[0] = apt[warp][kt_hi - k][g];
               en[1] = apt[warp][kt_hi - k][g + 8];
-              // H <- H t
+              // H <- H t (derivative chains: Q <- (Q + P) t, P <- P t)
 #pragma unroll
               for (int j = 0; j < 3; ++j)
 #pragma unroll
                 for (int V = 0; V < 2; ++V) {
                   const float hr = H[j][2 * V], hi = H[j][2 * V + 1];
                   const float2 t = tph[V][j];
+                  if constexpr (DERIV) {
+                    const float qr = HQ[j][2 * V] + hr, qi = HQ[j][2 * V + 1] + hi;
+                    HQ[j][2 * V] = fmaf(qr, t.x, -qi * t.y);
+                    HQ[j][2 * V + 1] = fmaf(qr, t.y, qi * t.x);
+                    const float pr2 = HP[j][2 * V], pi2 = HP[j][2 * V + 1];
+                    const float sr = HPQ[j][2 * V] + pr2, si = HPQ[j][2 * V + 1] + pi2;
+                    HPQ[j][2 * V] = fmaf(sr, t.x, -si * t.y);
+                    HPQ[j][2 * V + 1] = fmaf(sr, t.y, si * t.x);
+                    HP[j][2 * V] = fmaf(pr2, t.x, -pi2 * t.y);
+                    HP[j][2 * V + 1] = fmaf(pr2, t.y, pi2 * t.x);
+                  }
                   H[j][2 * V] = fmaf(hr, t.x, -hi * t.y);
                   H[j][2 * V + 1] = fmaf(hr, t.y, hi * t.x);
                 }
@@ -1349,24 +1390,67 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
                 for (int j = 0; j < 3; ++j) tc_mma(H[j], ah, bf[j].z, bf[j].w);
 #pragma unroll
                 for (int j = 0; j < 3; ++j) tc_mma(H[j], al, bf[j].x, bf[j].y);
+                if constexpr (DERIV) {
+                  // the second product: A scaled by the pairs' receive delays
+                  unsigned ah2[4], al2[4];
+#pragma unroll
+                  for (int V = 0; V < 2; ++V) {
+                    const float2 uu = make_float2(dsh->s_urx[2 * TC_KS * V + 2 * s][tid],
+                                                  dsh->s_urx[2 * TC_KS * V + 2 * s + 1][tid]);
+                    const float2 r2 = __fmul2_rn(rre[V], uu), i2 = __fmul2_rn(rim[V], uu);
+                    tc_split(r2.x, r2.y, ah2[V], al2[V]);
+                    tc_split(i2.x, i2.y, ah2[2 + V], al2[2 + V]);
+                  }
+#pragma unroll
+                  for (int j = 0; j < 3; ++j) tc_mma(HP[j], ah2, bf[j].x, bf[j].y);
+#pragma unroll
+                  for (int j = 0; j < 3; ++j) tc_mma(HP[j], ah2, bf[j].z, bf[j].w);
+#pragma unroll
+                  for (int j = 0; j < 3; ++j) tc_mma(HP[j], al2, bf[j].x, bf[j].y);
+                }
               }
             }
           }
           // flush: the image gains t^{kc_lo} H with the exact phase
 #pragma unroll
           for (int V = 0; V < 2; ++V) {
-            float2 part = make_float2(0.0f, 0.0f);
+            float2 part = make_float2(0.0f, 0.0f), dpart = make_float2(0.0f, 0.0f);
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
               const int a = a0 + 4 * j + q;
               if (a < d.na) {
-                const float2 c = cis_ku(kc_lo, df_add(d.tx_ax[(size_t)a * d.nx + vic[V]],
-                                                      d.tx_az[(size_t)a * d.nz + vjc[V]]));
+                const dfl ut = df_add(d.tx_ax[(size_t)a * d.nx + vic[V]], d.tx_az[(size_t)a * d.nz + vjc[V]]);
+                const float2 c = cis_ku(kc_lo, ut);
                 const float2 t = cmul(c, make_float2(H[j][2 * V], H[j][2 * V + 1]));
                 part.x += t.x;
                 part.y += t.y;
+                if constexpr (DERIV) {
+                  // t^kc_lo [U_tx (kc_lo P + Q) + (kc_lo P' + Q')]
+                  const float utx = (ut.x - d.t0N) + ut.y, kl = (float)kc_lo;
+                  const float yr = utx * fmaf(kl, H[j][2 * V], HQ[j][2 * V]) + fmaf(kl, HP[j][2 * V], HPQ[j][2 * V]);
+                  const float yi =
+                      utx * fmaf(kl, H[j][2 * V + 1], HQ[j][2 * V + 1]) + fmaf(kl, HP[j][2 * V + 1], HPQ[j][2 * V + 1]);
+                  const float2 dt = cmul(c, make_float2(yr, yi));
+                  dpart.x += dt.x;
+                  dpart.y += dt.y;
+                }
               }
               H[j][2 * V] = H[j][2 * V + 1] = 0.0f;
+              if constexpr (DERIV) {
+                HQ[j][2 * V] = HQ[j][2 * V + 1] = HP[j][2 * V] = HP[j][2 * V + 1] = 0.0f;
+                HPQ[j][2 * V] = HPQ[j][2 * V + 1] = 0.0f;
+              }
+            }
+            if constexpr (DERIV) {
+              float4 b4 = dsh->s_dacc[V][tid];
+              float y = dpart.x - b4.z, t = b4.x + y;
+              b4.z = (t - b4.x) - y;
+              b4.x = t;
+              y = dpart.y - b4.w;
+              t = b4.y + y;
+              b4.w = (t - b4.y) - y;
+              b4.y = t;
+              dsh->s_dacc[V][tid] = b4;
             }
             float4 a4 = s_acc[V][tid];
             float y = part.x - a4.z, t = a4.x + y;
@@ -1391,6 +1475,15 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
       y += __shfl_xor_sync(0xffffffffu, y, 2);
       if (q == 0 && vvalid[V])
         image[(size_t)vic[V] * d.nz + vjc[V]] = make_float2(x * d.scale * inv_sigma, y * d.scale * inv_sigma);
+      if constexpr (DERIV) {
+        float dx = dsh->s_dacc[V][tid].x, dy = dsh->s_dacc[V][tid].y;
+        dx += __shfl_xor_sync(0xffffffffu, dx, 1);
+        dy += __shfl_xor_sync(0xffffffffu, dy, 1);
+        dx += __shfl_xor_sync(0xffffffffu, dx, 2);
+        dy += __shfl_xor_sync(0xffffffffu, dy, 2);
+        if (q == 0 && vvalid[V])
+          dimage[(size_t)vic[V] * d.nz + vjc[V]] = make_float2(dx * d.scale * inv_sigma, dy * d.scale * inv_sigma);
+      }
     }
     __syncthreads();
   }
@@ -1431,19 +1524,20 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
     __syncthreads();
     const int tile = s_tile;
     if (tile >= n_tiles) break;
-    pw_tc_tile<WIN>(d, tile, n_tiles_x, n_tiles_z, sh, lb_s, ub_s, ktop, image, weights, n_active, n_empty, n_exec);
+    pw_tc_tile<WIN, false>(d, tile, n_tiles_x, n_tiles_z, sh, lb_s, ub_s, ktop, image, weights, n_active, n_empty,
+                           n_exec);
   }
   pw_tc_flush_counts(d, n_active, n_empty, n_exec);
 }
 
 // One persistent launch over the tiles of many frames (a batch): each block draws
 // global tile numbers from the batch's counter, in frame order (the host orders the
-// frames largest first), finds the tile's frame, and runs pw_tc_tile on it with the
-// frame's descriptor copied to shared memory and the batch's segment scratch.
+// frames largest first), finds the tile's frame, and runs pw_tc_tile on it.  The frames'
+// descriptors stay in device memory (read through the cache; the host has set their
+// segment scratch to the batch's), which measured faster than a copy in shared memory.
 template <int WIN>
 __global__ void __launch_bounds__(NTHREADS, 4) pw_tc_batch_kernel(const PWBatchDev B) {
   __shared__ TcShared sh;
-  __shared__ PWDev sd;
   __shared__ int s_tile, s_frame;
   extern __shared__ __align__(16) unsigned char dyn[];  // lb[max_ne], ub[max_ne] (dfl), ktop[max_ne]
   dfl* lb_s = (dfl*)dyn;
@@ -1470,33 +1564,62 @@ __global__ void __launch_bounds__(NTHREADS, 4) pw_tc_batch_kernel(const PWBatchD
     __syncthreads();
     const int f = s_frame;
     if (f < 0) break;
+    const PWDev& d = B.frames[f];
     if (f != cur) {
-      if (cur >= 0) pw_tc_flush_counts(sd, n_active, n_empty, n_exec);
-      __syncthreads();   // every thread is done with the previous frame's descriptor
-      const int* src = reinterpret_cast<const int*>(B.frames + f);
-      int* dst = reinterpret_cast<int*>(&sd);
-      for (int w = tid; w < (int)(sizeof(PWDev) / sizeof(int)); w += NTHREADS) dst[w] = src[w];
-      __syncthreads();
-      if (tid == 0) {
-        sd.seg = B.seg;
-        sd.seg_cap = B.seg_cap;
-      }
-      for (int e = tid; e < sd.ne; e += NTHREADS) {
-        lb_s[e] = sd.el_lb[e];
-        ub_s[e] = sd.el_ub[e];
+      if (cur >= 0) pw_tc_flush_counts(B.frames[cur], n_active, n_empty, n_exec);
+      __syncthreads();   // every thread is done with the previous frame's element edges
+      for (int e = tid; e < d.ne; e += NTHREADS) {
+        lb_s[e] = d.el_lb[e];
+        ub_s[e] = d.el_ub[e];
       }
       cur = f;
     }
     for (int e = tid; e < B.max_ne; e += NTHREADS) ktop[e] = -1;
     if (tid == 0) {
-      sh.e_range[0] = sd.ne;
+      sh.e_range[0] = d.ne;
       sh.e_range[1] = -1;
     }
     __syncthreads();
-    const int ntx = (sd.nx + TC_TILE_X - 1) / TC_TILE_X, ntz = (sd.nz + TILE_Z - 1) / TILE_Z;
-    pw_tc_tile<WIN>(sd, s_tile, ntx, ntz, sh, lb_s, ub_s, ktop, B.images[f], B.weights[f], n_active, n_empty, n_exec);
+    const int ntx = (d.nx + TC_TILE_X - 1) / TC_TILE_X, ntz = (d.nz + TILE_Z - 1) / TILE_Z;
+    pw_tc_tile<WIN, false>(d, s_tile, ntx, ntz, sh, lb_s, ub_s, ktop, B.images[f], B.weights[f], n_active, n_empty,
+                           n_exec);
   }
-  if (cur >= 0) pw_tc_flush_counts(sd, n_active, n_empty, n_exec);
+  if (cur >= 0) pw_tc_flush_counts(B.frames[cur], n_active, n_empty, n_exec);
+}
+
+// The image and its derivative with respect to the speed of sound (see pw_tc_tile).
+template <int WIN>
+__global__ void __launch_bounds__(NTHREADS, 3)
+pw_tc_deriv_kernel(const PWDev d, float2* __restrict__ image, float2* __restrict__ dimage, int n_tiles_x,
+                   int n_tiles_z) {
+  __shared__ TcShared sh;
+  __shared__ TcDerivShared dsh;
+  __shared__ int s_tile;
+  extern __shared__ __align__(16) unsigned char dyn[];  // lb[ne], ub[ne] (dfl), ktop[ne]
+  dfl* lb_s = (dfl*)dyn;
+  dfl* ub_s = lb_s + d.ne;
+  int* ktop = (int*)(ub_s + d.ne);
+  const int tid = threadIdx.x;
+  const int n_tiles = n_tiles_x * n_tiles_z;
+  unsigned long long n_active = 0, n_empty = 0, n_exec = 0;
+  for (int e = tid; e < d.ne; e += NTHREADS) {
+    lb_s[e] = d.el_lb[e];
+    ub_s[e] = d.el_ub[e];
+  }
+  for (;;) {
+    if (tid == 0) s_tile = (int)atomicAdd(&d.counters[3], 1ull);
+    for (int e = tid; e < d.ne; e += NTHREADS) ktop[e] = -1;
+    if (tid == 0) {
+      sh.e_range[0] = d.ne;
+      sh.e_range[1] = -1;
+    }
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= n_tiles) break;
+    pw_tc_tile<WIN, true>(d, tile, n_tiles_x, n_tiles_z, sh, lb_s, ub_s, ktop, image, nullptr, n_active, n_empty,
+                          n_exec, &dsh, dimage);
+  }
+  pw_tc_flush_counts(d, n_active, n_empty, n_exec);
 }
 
 typedef void (*pw_kernel_t)(const PWDev, float2*, float*, int, int);
@@ -1615,6 +1738,34 @@ cudaError_t launch_pw_tc_prep(const PWDev& d, cudaStream_t s) {
   const int n_ap = (d.na + TC_NA - 1) / TC_NA;
   const size_t n = (size_t)n_ap * d.K * d.tc_S * 96;
   tc_prep_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, n_ap);
+  return cudaGetLastError();
+}
+
+typedef void (*pw_tc_deriv_t)(const PWDev, float2*, float2*, int, int);
+static pw_tc_deriv_t pw_tc_deriv_pick(int window_id) {
+  switch (window_id) {
+    case 0: return pw_tc_deriv_kernel<0>;
+    case 1: return pw_tc_deriv_kernel<1>;
+    case 2: return pw_tc_deriv_kernel<2>;
+    default: return pw_tc_deriv_kernel<4>;
+  }
+}
+
+cudaError_t launch_pw_tc_deriv(const PWDev& d, float2* image, float2* dimage, cudaStream_t s) {
+  if (!d.tc_B || !d.tc_max) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(d.counters, 0, 5 * sizeof(unsigned long long), s);
+  if (e == cudaSuccess) e = launch_pw_tc_prep(d, s);
+  if (e != cudaSuccess) return e;
+  const size_t smem = (size_t)d.ne * (sizeof(int) + 2 * sizeof(dfl));
+  int dev = 0, nsm = 0, bps = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pw_tc_deriv_pick(d.window_id), NTHREADS, smem);
+  if (bps < 1) bps = 1;
+  const int ntx = (d.nx + TC_TILE_X - 1) / TC_TILE_X, ntz = (d.nz + TILE_Z - 1) / TILE_Z;
+  // the plan's segment scratch holds pw_fused_max_grid blocks: at least this many
+  const int grid = min(min(ntx * ntz, nsm * bps), pw_fused_max_grid(d));
+  pw_tc_deriv_pick(d.window_id)<<<grid, NTHREADS, smem, s>>>(d, image, dimage, ntx, ntz);
   return cudaGetLastError();
 }
 
@@ -2550,136 +2701,14 @@ __global__ void __launch_bounds__(256) pw_sharp_sums_kernel(const float2* __rest
   }
 }
 
-// One block per (band bin k, slice of ADJ_SLICE voxels), one thread per element
-// (elements beyond the block size run as further passes), ADJ_NA angles per
-// pass.  Voxels are taken in batches of ADJ_VB: the block first stages, per
-// voxel, what every element shares -- the transmit phasors e^{j 2 pi k u_tx} of
-// the pass's angles, the aperture at bin k, 1/W and G -- then each thread adds
-// its element's terms: one exact receive phasor e^{j 2 pi k u_rx} per (voxel,
-// element) times the staged transmit phasors.  A slice is summed in FP32 and
-// the slices are added in FP64 (atomics into acc, finished by
-// pw_adjoint_finish_kernel).
-constexpr int ADJ_NA = 11;
-constexpr int ADJ_VB = 128;
-constexpr int ADJ_SLICE = 8192;   // voxels per block: the grid is bins x voxel slices
-template <int WIN>
-__global__ void __launch_bounds__(128, 4)
-pw_adjoint_kernel(const PWDev d, const float2* __restrict__ cot, const float* __restrict__ invw, float t0N,
-                  double* __restrict__ acc) {
-  __shared__ float2 sT[ADJ_VB][ADJ_NA];   // transmit phasor
-  __shared__ float sUt[ADJ_VB][ADJ_NA];   // u_tx - t0/N
-  __shared__ float2 sG[ADJ_VB];           // G_v / W_{v,k} (0: no contribution)
-  __shared__ int sAp[ADJ_VB][3];          // i_lb, i_ub, first element right of x
-  __shared__ int sCol[ADJ_VB], sRow[ADJ_VB];
-  const int tid = threadIdx.x;
-  const int kk = blockIdx.x, k = d.k_lb + kk;
-  const dfl g = d.g[kk];
-  const long long nvox_all = (long long)d.nx * d.nz;
-  const long long v_begin = (long long)blockIdx.y * ADJ_SLICE;
-  const long long nvox = min(nvox_all, v_begin + ADJ_SLICE);   // this slice: v_begin .. nvox - 1
-  const float inv_par = (d.window_par > 0.0f) ? 1.0f / d.window_par : 0.0f;
-  for (int e0 = 0; e0 < d.ne; e0 += 128) {
-    const int e = e0 + tid;
-    const bool has_e = e < d.ne;
-    const int ec = min(e, d.ne - 1);
-    const dfl cm = d.el_m[ec], cu = d.el_u[ec];
-    for (int a0 = 0; a0 < d.na; a0 += ADJ_NA) {
-      const int nag = min(ADJ_NA, d.na - a0);
-      // the slice's sums in FP32 (at most ADJ_SLICE voxels), added across slices in FP64
-      float pXr[ADJ_NA], pXi[ADJ_NA], pHr[ADJ_NA], pHi[ADJ_NA];
-#pragma unroll
-      for (int q = 0; q < ADJ_NA; ++q) pXr[q] = pXi[q] = pHr[q] = pHi[q] = 0.0f;
-      for (long long v0 = v_begin; v0 < nvox; v0 += ADJ_VB) {
-        const int nvb = (int)min((long long)ADJ_VB, nvox - v0);
-        __syncthreads();  // the previous batch is consumed
-        for (int q = tid; q < nvb; q += 128) {
-          const long long v = v0 + q;
-          const int i = (int)(v / d.nz), j = (int)(v - (long long)i * d.nz);
-          int ilb, iub;
-          aperture(d.col_p[i], d.row_p[j], g, d.ne, ilb, iub);
-          const float iw = invw[(size_t)v * d.K + kk];
-          const float2 G = cot[v];
-          sG[q] = make_float2(G.x * iw, G.y * iw);
-          sAp[q][0] = ilb;
-          sAp[q][1] = iub;
-          sAp[q][2] = d.col_emid[i];
-          sCol[q] = i;
-          sRow[q] = j;
-        }
-        for (int q = tid; q < nvb * nag; q += 128) {
-          const int vb = q / nag, a = q - vb * nag, aa = a0 + a;
-          const long long v = v0 + vb;
-          const int i = (int)(v / d.nz), j = (int)(v - (long long)i * d.nz);
-          const dfl ut = df_add(d.tx_ax[(size_t)aa * d.nx + i], d.tx_az[(size_t)aa * d.nz + j]);
-          sT[vb][a] = cis_ku(k, ut);
-          sUt[vb][a] = (ut.x - t0N) + ut.y;
-        }
-        __syncthreads();
-        if (!has_e) continue;
-        for (int vb = 0; vb < nvb; ++vb) {
-          const float2 G = sG[vb];
-          if (G.x == 0.0f && G.y == 0.0f) continue;
-          const int ilb = sAp[vb][0], iub = sAp[vb][1];
-          const bool left = e < sAp[vb][2];
-          if (left ? (e < ilb) : (e > iub)) continue;
-          const int i = sCol[vb], j = sRow[vb];
-          const dfl xm = d.col_m[i];
-          float L;
-          if (left) {
-            const dfl l = d.el_lb[ilb];
-            L = (xm.x - l.x) + (xm.y - l.y);
-          } else {
-            const dfl u = d.el_ub[iub];
-            L = (u.x - xm.x) + (u.y - xm.y);
-          }
-          const float b = win_t<WIN>(d.window_par, inv_par, fabsf((cm.x - xm.x) + (cm.y - xm.y)) / L);
-          if (b == 0.0f) continue;
-          const float Gr = G.x * b, Gi = G.y * b;
-          const dfl urx = df_sqrt(df_add(df_sqr(df_sub(cu, d.col_u[i])), d.row_u2[j]));
-          const float2 P = cis_ku(k, urx);
-          const float ur = urx.x + urx.y;
-          // term = G b conj(P T) = (G b conj(P)) conj(T)
-          const float Qr = fmaf(Gr, P.x, Gi * P.y), Qi = fmaf(Gi, P.x, -Gr * P.y);
-#pragma unroll
-          for (int a = 0; a < ADJ_NA; ++a) {
-            if (a < nag) {
-              const float2 T = sT[vb][a];
-              const float Tr = fmaf(Qr, T.x, Qi * T.y), Ti = fmaf(Qi, T.x, -Qr * T.y);
-              const float U = ur + sUt[vb][a];
-              pXr[a] += Tr;
-              pXi[a] += Ti;
-              pHr[a] = fmaf(Tr, U, pHr[a]);
-              pHi[a] = fmaf(Ti, U, pHi[a]);
-            }
-          }
-        }
-      }
-      if (has_e) {
-#pragma unroll
-        for (int a = 0; a < ADJ_NA; ++a) {
-          if (a < nag) {
-            double* o = acc + 4 * (((size_t)e * d.K + kk) * d.na + a0 + a);
-            atomicAdd(o, (double)pXr[a]);
-            atomicAdd(o + 1, (double)pXi[a]);
-            atomicAdd(o + 2, (double)pHr[a]);
-            atomicAdd(o + 3, (double)pHi[a]);
-          }
-        }
-      }
-    }
-  }
-}
-
-// dL/dc = sum_{e,k,a} coef k Im(X conj(H)),  coef = 4 pi (2/N) / c
-__global__ void __launch_bounds__(256) pw_dldc_kernel(const PWDev d, const float2* __restrict__ H, double coef,
-                                                      double* __restrict__ out) {
+// dL/dc = coef sum_v Im(conj(G_v) Draw_v), coef = 4 pi / c (dI/dc = -(2 pi i / c) Draw)
+__global__ void __launch_bounds__(256) pw_dc_reduce_kernel(const float2* __restrict__ G, const float2* __restrict__ D,
+                                                           long long n, double coef, double* __restrict__ out) {
   __shared__ double r[8];
   double s = 0.0;
-  const long long n = (long long)d.ne * d.K * d.na;
   for (long long i = (long long)blockIdx.x * 256 + threadIdx.x; i < n; i += (long long)gridDim.x * 256) {
-    const int kk = (int)((i / d.na) % d.K);
-    const float2 x = d.X[i], h = H[i];
-    s += (double)(d.k_lb + kk) * ((double)x.y * h.x - (double)x.x * h.y);
+    const float2 g = G[i], dv = D[i];
+    s += (double)g.x * dv.y - (double)g.y * dv.x;
   }
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if ((threadIdx.x & 31) == 0) r[threadIdx.x >> 5] = s;
@@ -2710,16 +2739,6 @@ cudaError_t launch_pw_sharp_sums(const float2* img, long long n, double* sums, c
   return cudaGetLastError();
 }
 
-// FP64 sums {Xr, Xi, Hr, Hi} per (element, bin, angle) -> dL/dX* (scaled by 2/N) and H
-__global__ void __launch_bounds__(256) pw_adjoint_finish_kernel(const double* __restrict__ acc, size_t n, double scale,
-                                                                float2* __restrict__ gX, float2* __restrict__ H) {
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const double* a = acc + 4 * i;
-    gX[i] = make_float2((float)(scale * a[0]), (float)(scale * a[1]));
-    H[i] = make_float2((float)a[2], (float)a[3]);
-  }
-}
-
 // cotangent of the sharpness loss L = -S4 / S2^2: dL/dI*_v = -2 I_v (|I_v|^2 / S2^2 - S4 / S2^3)
 __global__ void __launch_bounds__(256) pw_sharp_cotangent_kernel(const float2* __restrict__ img, long long n, float gs2,
                                                                  float gs4, float2* __restrict__ G) {
@@ -2735,29 +2754,269 @@ cudaError_t launch_pw_sharp_cotangent(const float2* img, long long n, float gs2,
   return cudaGetLastError();
 }
 
-cudaError_t launch_pw_adjoint(const PWDev& d, const float2* cot, const float* invw, float t0N, float2* gX, float2* H,
+// fp16 scale of Q = conj(t^k) G / W: the power of two that brings max|G| max(1/W), a bound
+// of |Q|, below 2^14 (gmax: float bits of max |G component| and of max 1/W)
+__device__ __forceinline__ float adj_scale(const unsigned* gmax) {
+  const float m = __uint_as_float(gmax[0]) * __uint_as_float(gmax[1]);
+  if (!(m > 0.0f) || !(m < 3.0e38f)) return 1.0f;
+  int ex;
+  frexpf(m, &ex);
+  return ldexpf(1.0f, min(max(14 - ex, -126), 126));
+}
+
+// largest |x| of n floats (float bits, >= 0 floats order as integers) into *out
+__global__ void __launch_bounds__(256) absmax_f32_kernel(const float* __restrict__ x, size_t n, unsigned* out) {
+  float m = 0.0f;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(x[i]));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+// FP64 sums {Xr, Xi} per (element, bin, angle) -> dL/dX* (scaled by 2/N, the fp16 scale undone)
+__global__ void __launch_bounds__(256) pw_adjoint_finish_kernel(const double* __restrict__ acc, size_t n, double scale,
+                                                                const unsigned* __restrict__ gmax,
+                                                                float2* __restrict__ gX) {
+  const double sc = scale / (double)adj_scale(gmax);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double* a = acc + 2 * i;
+    gX[i] = make_float2((float)(sc * a[0]), (float)(sc * a[1]));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The adjoint on the tensor cores: per band bin k,
+//   gX_k(e, a) = s sum_v conj(R_k(v, e)) Q_k(v, a),  R_k = b r^k,  Q_k = conj(t_va^k) G_v / W_vk,
+// an [elements x voxels] . [voxels x angles] product reduced over the voxels (the
+// forward's product transposed).  Block: 8 warps, warp w owns elements 16w..16w+15 of
+// the block's element pass (mma rows); the voxels are the mma k dimension (8 complex per
+// k-step, real form: columns 0..7 Re, 8..15 Im of conj(R)) and the angles the n dimension
+// (3 tiles of 4).  A block takes one chunk of ADJ_TB bins and one slice of voxels; per
+// group of 8 voxels it stages the aperture data and the B fragments of Q (fp16 hi and lo,
+// scaled by a power of two) in shared memory, then each warp forms conj(R) for its 16
+// elements x 8 voxels -- the receive phasor anchored exactly at the chunk's top bin and
+// stepped down by r -- and accumulates the chunk's bins in registers (ADJ_TB x 12 floats).
+// At the end of the slice the sums are added to FP64 accumulators.
+constexpr int ADJ_TB = 4;           // bins per chunk (register accumulators per bin)
+constexpr int ADJ_TC_SLICE = 8192;  // voxels per block
+constexpr int ADJ_TC_WARPS = 8;
+
+template <int WIN>
+__global__ void __launch_bounds__(ADJ_TC_WARPS * 32, 2)
+pw_adjoint_tc_kernel(const PWDev d, const float2* __restrict__ cot, const float* __restrict__ invw,
+                     const unsigned* __restrict__ gmax, double* __restrict__ acc) {
+  __shared__ float2 sQ[ADJ_TB][8][TC_NA];        // Q_k(v, a) sigma
+  __shared__ uint4 sB[ADJ_TB][3][32];            // B fragments {b0 hi, b1 hi, b0 lo, b1 lo}
+  __shared__ float2 sAp[ADJ_TB][8];              // {1/L_left, 1/L_right} per bin, voxel (1e30: no side)
+  __shared__ int sVox[8][3];                     // column, row, first element right of x
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, q = lane & 3;
+  const int kc_lo = d.k_lb + blockIdx.x * ADJ_TB, kc_hi = min(kc_lo + ADJ_TB, d.k_ub + 1) - 1;
+  const int nb = kc_hi - kc_lo + 1;
+  const long long nvox = (long long)d.nx * d.nz;
+  const long long v_begin = (long long)blockIdx.y * ADJ_TC_SLICE;
+  const long long v_end = min(nvox, v_begin + ADJ_TC_SLICE);
+  const int e_pass = blockIdx.z * (ADJ_TC_WARPS * 16);
+  const int eA = e_pass + 16 * warp + g, eB = eA + 8;   // the thread's elements (mma rows g, g + 8)
+  const dfl cmA = d.el_m[min(eA, d.ne - 1)], cmB = d.el_m[min(eB, d.ne - 1)];
+  const dfl cuA = d.el_u[min(eA, d.ne - 1)], cuB = d.el_u[min(eB, d.ne - 1)];
+  const float inv_par = (d.window_par > 0.0f) ? 1.0f / d.window_par : 0.0f;
+  const float sigma = adj_scale(gmax);
+  float C[ADJ_TB][3][4];
+#pragma unroll
+  for (int b = 0; b < ADJ_TB; ++b)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) C[b][j][0] = C[b][j][1] = C[b][j][2] = C[b][j][3] = 0.0f;
+
+  for (long long v0 = v_begin; v0 < v_end; v0 += 8) {
+    const int nv = (int)min(8ll, v_end - v0);
+    __syncthreads();   // the previous group's tables are consumed
+    if (tid < 8) {
+      const long long v = v0 + min(tid, nv - 1);
+      const int i = (int)(v / d.nz), j = (int)(v - (long long)i * d.nz);
+      sVox[tid][0] = i;
+      sVox[tid][1] = j;
+      sVox[tid][2] = d.col_emid[i];
+    }
+    __syncthreads();
+    // Q (96 threads: voxel x angle) and the aperture data (ADJ_TB x 8 threads)
+    if (tid < 8 * TC_NA) {
+      const int vv = tid / TC_NA, a = tid - vv * TC_NA;
+      float2 base = make_float2(0.0f, 0.0f), t = make_float2(1.0f, 0.0f);
+      if (vv < nv && a < d.na) {
+        const int i = sVox[vv][0], j = sVox[vv][1];
+        const dfl ut = df_add(d.tx_ax[(size_t)a * d.nx + i], d.tx_az[(size_t)a * d.nz + j]);
+        const float2 c = cis_ku(kc_hi, ut);
+        const float2 G = cot[v0 + vv];
+        t = cis_ku(1, ut);
+        // conj(t^k) G sigma at the top bin; going down, conj(t^(k-1)) = conj(t^k) t
+        base = make_float2(sigma * (G.x * c.x + G.y * c.y), sigma * (G.y * c.x - G.x * c.y));
+      }
+#pragma unroll
+      for (int b = 0; b < ADJ_TB; ++b) {
+        float2 qv = make_float2(0.0f, 0.0f);
+        if (vv < nv && a < d.na && b < nb) {
+          const float iw = invw[(size_t)(v0 + vv) * d.K + (kc_hi - b - d.k_lb)];
+          qv = make_float2(base.x * iw, base.y * iw);
+        }
+        sQ[b][vv][a] = qv;
+        base = cmul(base, t);
+      }
+    } else if (tid >= 128 && tid < 128 + ADJ_TB * 8) {
+      const int b = (tid - 128) >> 3, vv = (tid - 128) & 7;
+      float il = 1.0e30f, ir = 1.0e30f;
+      if (vv < nv && b < nb) {
+        const int i = sVox[vv][0], j = sVox[vv][1];
+        const dfl xm = d.col_m[i];
+        int ilb, iub;
+        aperture(d.col_p[i], d.row_p[j], d.g[kc_hi - b - d.k_lb], d.ne, ilb, iub);
+        if (ilb < d.ne) {
+          const dfl l = d.el_lb[ilb];
+          const float L = (xm.x - l.x) + (xm.y - l.y);
+          if (L > 0.0f) il = __fdividef(1.0f, L);
+        }
+        if (iub >= 0) {
+          const dfl u = d.el_ub[iub];
+          const float L = (u.x - xm.x) + (u.y - xm.y);
+          if (L > 0.0f) ir = __fdividef(1.0f, L);
+        }
+      }
+      sAp[b][vv] = make_float2(il, ir);
+    }
+    __syncthreads();
+    // B fragments: lane (gg, qq) of n-tile j holds rows 2qq, 2qq+1 (voxels, Re block) and
+    // 2qq+8, 2qq+9 (second block) of column gg = angle 4j + gg/2, part gg%2
+    for (int f = tid; f < ADJ_TB * 3 * 32; f += ADJ_TC_WARPS * 32) {
+      const int b = f / 96, j = (f / 32) % 3, ln = f & 31;
+      const int gg = ln >> 2, qq = ln & 3, a = 4 * j + (gg >> 1), part = gg & 1;
+      float r0[2], r1[2];
+#pragma unroll
+      for (int t2 = 0; t2 < 2; ++t2) {
+        const float2 qv = sQ[b][2 * qq + t2][a];
+        r0[t2] = part ? qv.y : qv.x;     // rows 0..7:  Re Q (column re) / Im Q (column im)
+        r1[t2] = part ? qv.x : -qv.y;    // rows 8..15: -Im Q / Re Q
+      }
+      uint4 o;
+      tc_split(r0[0], r0[1], o.x, o.z);
+      tc_split(r1[0], r1[1], o.y, o.w);
+      sB[b][j][ln] = o;
+    }
+    __syncthreads();
+    // conj(R) of elements (eA, eB) x voxels (2q, 2q+1)
+    float2 P[2][2], st[2][2];   // [element][voxel]: conj(r^k) and the step r
+    float dl[2][2], dr[2][2];   // distances to the voxel by aperture side
+#pragma unroll
+    for (int t2 = 0; t2 < 2; ++t2) {
+      const int vv = 2 * q + t2;
+      const int i = sVox[vv][0], j = sVox[vv][1];
+      const dfl xm = d.col_m[i], xu = d.col_u[i], zu2 = d.row_u2[j];
+      const int emid = sVox[vv][2];
+#pragma unroll
+      for (int m = 0; m < 2; ++m) {
+        const dfl cm = m ? cmB : cmA, cu = m ? cuB : cuA;
+        const int e = m ? eB : eA;
+        const dfl urx = df_sqrt(df_add(df_sqr(df_sub(cu, xu)), zu2));
+        const float2 c = cis_ku(kc_hi, urx);
+        P[m][t2] = make_float2(c.x, -c.y);
+        st[m][t2] = cis_ku(1, urx);
+        const float dx = fabsf((cm.x - xm.x) + (cm.y - xm.y));
+        const bool ok = (vv < nv) && (e < d.ne);
+        const bool left = e < emid;
+        dl[m][t2] = ok ? (left ? dx : 0.0f) : 1.0e30f;   // an empty slot lies outside every aperture
+        dr[m][t2] = ok ? (left ? 0.0f : dx) : 0.0f;
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < ADJ_TB; ++b) {
+      if (b < nb) {
+        float rr[2][2], ri[2][2];
+#pragma unroll
+        for (int t2 = 0; t2 < 2; ++t2) {
+          const float2 ap = sAp[b][2 * q + t2];
+#pragma unroll
+          for (int m = 0; m < 2; ++m) {
+            const float u = fmaf(dl[m][t2], ap.x, dr[m][t2] * ap.y);
+            const float w = (u < 1.0f) ? win_t<WIN>(d.window_par, inv_par, u) : 0.0f;
+            const float2 pc = P[m][t2];
+            rr[m][t2] = w * pc.x;          // Re conj(R)
+            ri[m][t2] = w * pc.y;          // Im conj(R)
+            P[m][t2] = cmul(pc, st[m][t2]);
+          }
+        }
+        unsigned ah[4], al[4];
+        tc_split(rr[0][0], rr[0][1], ah[0], al[0]);   // row g:     columns 2q, 2q+1
+        tc_split(rr[1][0], rr[1][1], ah[1], al[1]);   // row g + 8
+        tc_split(ri[0][0], ri[0][1], ah[2], al[2]);   // row g:     columns 2q+8, 2q+9
+        tc_split(ri[1][0], ri[1][1], ah[3], al[3]);   // row g + 8
+        uint4 bf[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) bf[j] = sB[b][j][lane];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) tc_mma(C[b][j], ah, bf[j].x, bf[j].y);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) tc_mma(C[b][j], ah, bf[j].z, bf[j].w);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) tc_mma(C[b][j], al, bf[j].x, bf[j].y);
+      }
+    }
+  }
+  // C[b][j]: rows g, g+8 (elements eA, eB), columns 2q, 2q+1 (angle 4j + q: re, im)
+#pragma unroll
+  for (int b = 0; b < ADJ_TB; ++b) {
+    if (b >= nb) continue;
+    const int kk = kc_hi - b - d.k_lb;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int a = 4 * j + q;
+      if (a >= d.na) continue;
+#pragma unroll
+      for (int m = 0; m < 2; ++m) {
+        const int e = m ? eB : eA;
+        if (e >= d.ne) continue;
+        double* o = acc + 2 * (((size_t)e * d.K + kk) * d.na + a);
+        atomicAdd(o, (double)C[b][j][2 * m]);
+        atomicAdd(o + 1, (double)C[b][j][2 * m + 1]);
+      }
+    }
+  }
+}
+
+cudaError_t launch_pw_adjoint(const PWDev& d, const float2* cot, const float* invw, unsigned* gmax, float2* gX,
                               double* acc, cudaStream_t s) {
   const size_t n = (size_t)d.ne * d.K * d.na;
-  cudaError_t e = cudaMemsetAsync(acc, 0, 4 * n * sizeof(double), s);
-  if (e != cudaSuccess) return e;
   const long long nvox = (long long)d.nx * d.nz;
-  const dim3 grid(d.K, (unsigned)((nvox + ADJ_SLICE - 1) / ADJ_SLICE));
+  // gmax[1] (max 1/W) is set once with the 1/W table; max |G| per call
+  cudaError_t e = cudaMemsetAsync(acc, 0, 2 * n * sizeof(double), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(gmax, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
+  absmax_f32_kernel<<<608, 256, 0, s>>>(reinterpret_cast<const float*>(cot), 2 * (size_t)nvox, gmax);
+  const dim3 grid((d.K + ADJ_TB - 1) / ADJ_TB, (unsigned)((nvox + ADJ_TC_SLICE - 1) / ADJ_TC_SLICE),
+                  (d.ne + ADJ_TC_WARPS * 16 - 1) / (ADJ_TC_WARPS * 16));
+  const int nt = ADJ_TC_WARPS * 32;
   switch (d.window_id) {
-    case 0: pw_adjoint_kernel<0><<<grid, 128, 0, s>>>(d, cot, invw, t0N, acc); break;
-    case 1: pw_adjoint_kernel<1><<<grid, 128, 0, s>>>(d, cot, invw, t0N, acc); break;
-    case 2: pw_adjoint_kernel<2><<<grid, 128, 0, s>>>(d, cot, invw, t0N, acc); break;
-    default: pw_adjoint_kernel<4><<<grid, 128, 0, s>>>(d, cot, invw, t0N, acc); break;
+    case 0: pw_adjoint_tc_kernel<0><<<grid, nt, 0, s>>>(d, cot, invw, gmax, acc); break;
+    case 1: pw_adjoint_tc_kernel<1><<<grid, nt, 0, s>>>(d, cot, invw, gmax, acc); break;
+    case 2: pw_adjoint_tc_kernel<2><<<grid, nt, 0, s>>>(d, cot, invw, gmax, acc); break;
+    default: pw_adjoint_tc_kernel<4><<<grid, nt, 0, s>>>(d, cot, invw, gmax, acc); break;
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  pw_adjoint_finish_kernel<<<608, 256, 0, s>>>(acc, n, (double)d.scale, gX, H);
+  pw_adjoint_finish_kernel<<<608, 256, 0, s>>>(acc, n, (double)d.scale, gmax, gX);
   return cudaGetLastError();
 }
 
-cudaError_t launch_pw_dldc(const PWDev& d, const float2* H, double coef, double* out, cudaStream_t s) {
+cudaError_t launch_absmax(const float* x, size_t n, unsigned* out, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
+  absmax_f32_kernel<<<608, 256, 0, s>>>(x, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pw_dc_reduce(const float2* G, const float2* D, long long n, double coef, double* out,
+                               cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), s);
   if (e != cudaSuccess) return e;
-  pw_dldc_kernel<<<608, 256, 0, s>>>(d, H, coef, out);
+  pw_dc_reduce_kernel<<<608, 256, 0, s>>>(G, D, n, coef, out);
   return cudaGetLastError();
 }
 
