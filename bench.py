@@ -57,7 +57,9 @@ def parse():
     ap.add_argument("--frames", type=int, default=64, help="batch: frames per batch")
     ap.add_argument("--no-autotune", action="store_true", help="batch: keep each plan's default kernel variant")
     ap.add_argument("--variant", type=int, default=0,
-                    help="cpwc: pin the plane-wave kernel variant (fnum_plan_set_kernel_variant; 0 = the default)")
+                    help="cpwc / saft: pin the kernel variant (fnum_plan_set_kernel_variant; 0 = the default; "
+                    "saft: 1 recurrence kernels, 2 tensor cores)")
+    ap.add_argument("--no-accuracy", action="store_true", help="saft: skip the error against the FP64 oracle")
     ap.add_argument("--band", default="full", choices=["full", "2-7"],
                     help="saft band: the gateway default [DBL_MIN, f_s/2] or 2-7 MHz")
     return ap.parse_args()
@@ -165,6 +167,39 @@ def accuracy_of(wl, win, fn, img, n_random=192, n_bright=64):
             "sample": "%d seeded random voxels + the %d brightest of the frame" % (n_random, n_bright),
             "bmode": "20 |log10(|I| / |I_ref|)| on voxels above -40 dB of the frame maximum (a common "
                      "normaliser cancels)"}
+
+
+def measured_peaks():
+    """The machine's measured HBM and bf16 peaks (MEASURED_PEAKS.json beside this file), or {}."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def saft_accuracy_of(wl, fn, img, n_random=40, n_bright=16):
+    """Error of a SAFT frame (img: [n_x, n_z] complex) against the FP64 oracle (MEX
+    semantics, oracle/fnum_oracle.c) on seeded random voxels plus the brightest."""
+    from oracle import coracle as CO
+    nx, nz = img.shape
+    rng = np.random.default_rng(7)
+    flat = np.abs(img).ravel()
+    pick = np.unique(np.concatenate([rng.choice(nx * nz, n_random, replace=False), np.argsort(flat)[-n_bright:]]))
+    ix, iz = pick // nz, pick % nz
+    rf32 = np.asarray(wl.rf, dtype=np.float32).astype(np.float64)
+    ref, _, _, _ = CO.sa_mex(wl.positions_x, wl.positions_z, rf32, wl.f_s, wl.array.width, wl.array.pitch, wl.c,
+                             wl.f_bounds, 0.0, ("boxcar", 0.0), ("boxcar", 0.0), fn.spec(), fn.spec(), "on", "on",
+                             ix, iz)
+    got = img[ix, iz].astype(np.complex128)
+    thr = flat.max() * 10 ** (-40 / 20)
+    hi = np.abs(ref) > thr
+    dphi = np.abs(np.angle(got[hi] * np.conj(ref[hi])))
+    return {"rel_l2": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+            "max_phase_err_rad": float(dphi.max()) if dphi.size else None,
+            "voxels": int(pick.size), "voxels_above_-40dB": int(hi.sum()),
+            "against": "FP64 oracle (MEX semantics, oracle/fnum_oracle.c) on the float32 RF of the timed frame",
+            "sample": "%d seeded random voxels + the %d brightest of the frame" % (n_random, n_bright)}
 
 
 # ---------------------------------------------------------------------------
@@ -517,6 +552,8 @@ def run_saft(args):
     plan = das.SAPlan(wl.positions_x, wl.positions_z, wl.n_samples, wl.array.n_elements, wl.f_s, wl.array.width,
                       wl.array.pitch, wl.c, wl.f_bounds, 0.0, windows.boxcar(), windows.boxcar(), fn, fn,
                       device=local, kernel=args.kernel)
+    if args.variant:
+        plan.set_kernel_variant(args.variant)
     rf = torch.tensor(wl.rf, dtype=torch.float32, device=dev)                 # [tx, rx, t]
     img = torch.empty((1, plan.n_x, plan.n_z), dtype=torch.complex64, device=dev)
     stream = torch.cuda.current_stream()
@@ -543,12 +580,31 @@ def run_saft(args):
     _lib.check(_lib.lib().fnum_diag_fp32_peak(local, _lib.C.byref(peak)))
     active = info["active_terms"] if args.kernel == "fused" else info["terms"]
     achieved = 8.0 * active / (bf_ms * 1e-3) / 1e12
-    roof = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-            "frac": achieved / peak.value if peak.value else None, "traffic": None,
-            "kernel": "sa_event_kernel<12,boxcar> (boxcar receive window)" if args.kernel == "fused" else "sa_plain_kernel",
+    tc = args.kernel == "fused" and info["kernel_variant"] == 2
+    fp32 = {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+            "frac": achieved / peak.value if peak.value else None,
             "work": "8 FLOP per active voxel x tx x rx x bin term; %d active of %d nominal terms"
             % (info["active_terms"], info["terms"]),
             "peak_source": "measured FP32 FMA throughput (fnum_diag_fp32_peak)"}
+    if tc:
+        # tcgen05.mma work: per executed voxel x tx x rx x bin term of a tile's element range,
+        # 4 real products (real form) x 3 (fp16 hi.lo, lo.hi, hi.hi) x 2 FLOP
+        mflops = 24.0 * info["executed_terms"]
+        mpk = measured_peaks().get("bf16_tflops")
+        tach = mflops / (bf_ms * 1e-3) / 1e12
+        roof = {"bound": "tensor", "achieved": tach, "peak": mpk, "unit": "TFLOP/s",
+                "frac": tach / mpk if mpk else None, "traffic": None, "kernel": "sa_tc_kernel<boxcar,boxcar>",
+                "work": "24 FLOP per executed term (real-form complex product, three fp16 products); %d executed "
+                        "terms (tile element ranges x bins), %d active" % (info["executed_terms"], info["active_terms"]),
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS bf16 burst; fp16 runs at the bf16 rate)",
+                "fp32_equivalent": fp32}
+    else:
+        roof = dict(fp32, traffic=None,
+                    kernel="sa_event_kernel<12,boxcar> (boxcar receive window)" if args.kernel == "fused"
+                    else "sa_plain_kernel")
+    acc = None
+    if rank == 0 and not args.no_accuracy:
+        acc = saft_accuracy_of(wl, fn, img[0].cpu().numpy())
     if rank != 0:
         return
     out = {"metric": SA_METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
@@ -557,10 +613,11 @@ def run_saft(args):
            "config": saft_config(wl, args.kernel, args.band),
            "gterms_per_s": info["terms"] / (np.mean(step_ms) * 1e-3) / 1e9,
            "stage_ms": {"band_dft": float(np.mean([a.elapsed_time(b) for a, b, c in evs])), "beamform": bf_ms},
-           "roofline": roof, "clocks": clk,
-           # per step: the band DFT (operand split + tcgen05 GEMM), the symmetrisation kernel
-           # (when it applies) and the beamformer; no library kernels
-           "gpu_launches": args.steps * (4 if args.kernel == "fused" else 3),
+           "roofline": roof, "accuracy": acc, "kernel_variant": info["kernel_variant"], "clocks": clk,
+           # per step: the band DFT (operand split + tcgen05 GEMM), then either the spectra scale,
+           # the operand planes and the tensor-core beamformer, or the symmetrisation kernel and
+           # the recurrence beamformer (or the plain kernel); no library kernels
+           "gpu_launches": args.steps * (5 if tc else 4 if args.kernel == "fused" else 3),
            "library_launches": {}}
     print(json.dumps(out))
     plan.close()
@@ -692,36 +749,43 @@ def run_adjoint(args):
     b.record(stream)
     torch.cuda.synchronize()
     fwd_ms = a.elapsed_time(b)
-    # the adjoint alone (fnum_pw_adjoint: dL/dX* and dL/dc for a cotangent) on the frame's spectra
+    # the adjoint alone (fnum_pw_adjoint without dL/dc: pw_adjoint_tc_kernel and its scale and finishing
+    # kernels), then with dL/dc (adds the derivative forward pass and its reduction), on the frame's spectra
     cot = torch.randn((plan.n_x, plan.n_z), dtype=torch.complex64, device=dev)
-    plan.adjoint(cot, stream=stream)
-    adj = []
-    for _ in range(3):
-        a.record(stream)
-        plan.adjoint(cot, stream=stream)
-        b.record(stream)
-        torch.cuda.synchronize()
-        adj.append(a.elapsed_time(b))
-    adj_ms = float(np.mean(adj))
+
+    def timed(fn):
+        fn()
+        ts = []
+        for _ in range(3):
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.mean(ts))
+
+    adj_ms = timed(lambda: plan.adjoint(cot, dc=False, stream=stream))
+    adj_dc_ms = timed(lambda: plan.adjoint(cot, dc=True, stream=stream))
     info = plan.info()
     from f_number_gb300 import _lib
     peak = _lib.C.c_double(0.0)
     _lib.check(_lib.lib().fnum_diag_fp32_peak(0, _lib.C.byref(peak)))
-    # per active voxel x element x bin x angle term the adjoint forms two complex MACs:
-    # dL/dX* and the dL/dc sum H (16 FLOP)
-    adj_tflops = 16.0 * info["active_terms"] / (adj_ms * 1e-3) / 1e12
+    # per active voxel x element x bin x angle term the adjoint forms one complex MAC into dL/dX*
+    # (8 FLOP); the tensor cores do it, so the FP32 figure is an FP32-equivalent rate
+    adj_tflops = 8.0 * info["active_terms"] / (adj_ms * 1e-3) / 1e12
     roof = {"bound": "fp32", "achieved": adj_tflops, "peak": peak.value, "unit": "TFLOP/s",
             "frac": adj_tflops / peak.value if peak.value else None, "traffic": None,
-            "kernel": "pw_adjoint_kernel (+ dL/dc reduction)",
-            "work": "16 FLOP per active term (two complex MACs: dL/dX* and H); %d active terms"
-                    % info["active_terms"],
+            "kernel": "pw_adjoint_tc_kernel",
+            "work": "8 FLOP per active term (one complex MAC into dL/dX*, FP32-equivalent: the products run on "
+                    "the tensor cores); %d active terms" % info["active_terms"],
             "peak_source": "measured FP32 FMA throughput (fnum_diag_fp32_peak)"}
     out = {"metric": ADJ_METRIC, "value": args.steps / dt, "unit": "evaluations/s", "n_gpus": 1, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32 (double-float phase, FP64 reductions)", "data": "synthetic",
            "config": {"workload": "adjoint_cpwc_11angles_128el_2048smp_%dx%d_rf_at_1500" % (args.grid, args.grid),
                       "trial_c": 1500.0, "frozen_at_c": 1540.0},
-           "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "roofline": roof, "sweep": sweep, "clocks": clk}
+           "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "adjoint_with_dc_ms": adj_dc_ms,
+           "derivative_forward_ms": adj_dc_ms - adj_ms, "roofline": roof, "sweep": sweep, "clocks": clk}
     print(json.dumps(out))
     plan.close()
 

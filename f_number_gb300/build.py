@@ -13,7 +13,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libfnum.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["fnum_kernels.cu", "fnum_host.cpp", "fnum_diag.cu", "fnum_noalloc.cu", "fnum_post.cu", "fnum_dft_tc.cu"]
+SOURCES = ["fnum_kernels.cu", "fnum_host.cpp", "fnum_diag.cu", "fnum_noalloc.cu", "fnum_post.cu", "fnum_dft_tc.cu",
+           "fnum_sa_tc.cu"]
 
 
 def nvcc() -> str:

@@ -39,6 +39,7 @@
 #include <algorithm>
 
 #include "fnum_internal.h"
+#include "fnum_tc_ptx.cuh"
 
 namespace fnum {
 
@@ -53,85 +54,18 @@ constexpr int DT_STAGE_BYTES = 4 * DT_TILE_BYTES;  // A hi, A lo, B hi, B lo
 constexpr int DT_SMEM = DT_STAGES * DT_STAGE_BYTES + 1024 + 128;   // + alignment slack + barriers
 constexpr int DT_THREADS = 192;                    // producer, MMA issuer, four drain warps
 constexpr int DT_TMEM_COLS = 2 * DT_BN;            // two accumulators
-constexpr unsigned long long DT_WAIT_NS = 2000000000ull;
 
 static_assert(DT_BM == DT_BN, "the four operand tiles share one size");
 
-// instruction descriptor of tcgen05.mma kind::f16: fp32 accumulator (bits 4-5 = 1),
-// A and B fp16 (bits 7-9, 10-12 = 0), both K-major (bits 15, 16 = 0), N >> 3 at
-// bits 17-22, M >> 4 at bits 24-28
-constexpr uint32_t DT_IDESC = (1u << 4) | ((uint32_t)(DT_BN >> 3) << 17) | ((uint32_t)(DT_BM >> 4) << 24);
+constexpr uint32_t DT_IDESC = tcx::idesc_f16(DT_BM, DT_BN);
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-// waits for the phase of parity `parity` to complete; false after DT_WAIT_NS
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  const unsigned long long t0 = global_ns();
-  for (;;) {
-    uint32_t ok;
-    asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (ok) return true;
-    if (global_ns() - t0 > DT_WAIT_NS) return false;
-  }
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::
-          "r"(dst),
-      "l"((uint64_t)map), "r"(bar), "r"(x), "r"(y)
-      : "memory");
-}
-
-// shared-memory matrix descriptor: K-major tile of 64 fp16 per 128-byte row, rows
-// in 8-row groups of 1024 bytes (SBO), 128-byte swizzle (layout type 2 at bits
-// 61-63), descriptor version 1 at bits 46-47; LBO is not used by swizzled K-major
-// tiles (encoded 1)
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
-         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
-}
+using namespace tcx;
 
 __device__ __forceinline__ void tc_mma_f16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
-  asm volatile(
-      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-          tmem_d),
-      "l"(da), "l"(db), "r"(DT_IDESC), "r"(accumulate));
+  mma_f16(tmem_d, da, db, DT_IDESC, accumulate);
 }
 
-__device__ __forceinline__ void tc_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-        "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
-        "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
-        "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
+__device__ __forceinline__ void tc_commit(uint32_t bar) { mma_commit(bar); }
 
 // ---------------------------------------------------------------------------
 // operands
@@ -201,9 +135,6 @@ struct DftOut {
   int n_kb;                    // samples / DT_BK
 };
 
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
 
 __global__ void __launch_bounds__(DT_THREADS, 1)
 dft_tc_gemm_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant__ CUtensorMap tm_alo,
@@ -345,25 +276,6 @@ dft_tc_gemm_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_cons
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(DT_TMEM_COLS) : "memory");
   }
-}
-
-typedef CUresult (*EncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiled encode_fn() {
-  static EncodeTiled fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = (EncodeTiled)p;
-    else
-      (void)cudaGetLastError();
-  }
-  return fn;
 }
 
 // 2-D fp16 map over rows x Kp (K-major), 64 x 128 boxes, 128-byte swizzle; rows

@@ -458,6 +458,12 @@ struct fnum_plan {
   bool adj_invw_ready = false;
   // band DFT on the tensor cores: fp16 hi/lo operand planes, per-line scales, TMA maps
   fnum::DftTc dft{};
+  // synthetic aperture on the tensor cores: operand planes, TMA maps, scale word and
+  // time-offset phasors (when the plan qualifies), and the chosen variant
+  // (0: default = tensor cores when available, 1: recurrence kernels, 2: tensor cores)
+  fnum::SaTc satc{};
+  bool sa_tc_ok = false;
+  int sa_variant = 0;
   // device buffers of the host-buffer entry points (fnum_das_pw / fnum_das_sa), kept for the
   // plan's life so that a cached plan runs without allocating
   double* h_rf = nullptr;
@@ -830,6 +836,7 @@ int make_sa_plan(const fnum_sa_desc* d, int flags, fnum_plan** out) {
   D.seg_cap = (mono ? std::min(bk.K, 4 * ne + 32) : bk.K) + 1;  // + the sentinel entry
   D.flush_chunks = 4;
   D.scale = (float)(2.0 / b.N);
+  D.t0N = to_df(d->index_t0 / b.N);
   std::vector<dfl> gt, gr;
   g_table(Ftx, gt);
   g_table(Frx, gr);
@@ -878,6 +885,25 @@ int make_sa_plan(const fnum_sa_desc* d, int flags, fnum_plan** out) {
     P->info.scratch_bytes = (long long)P->grid * fnum::NTHREADS * D.seg_cap * fnum::SA_SEG_INT4 * (long long)sizeof(int4);
     if (D.Xs) P->info.scratch_bytes += (long long)ne * ne * bk.K * (long long)sizeof(float2);
   }
+  if (!(flags & FNUM_FLAG_PLAIN_KERNEL) && fnum::sa_tc_supported(D)) {
+    // operand planes of the tensor-core kernel and the phasors e^{2 pi i k t0 / N} of the band
+    unsigned short* planes = nullptr;
+    unsigned* mb = nullptr;
+    float2* rot = nullptr;
+    std::vector<float2> rv(bk.K);
+    for (int i = 0; i < bk.K; ++i) {
+      const double cyc = std::fmod((double)(bk.k_lb + i) * d->index_t0, (double)b.N) / (double)b.N;
+      rv[i] = make_float2((float)std::cos(2.0 * M_PI * cyc), (float)std::sin(2.0 * M_PI * cyc));
+    }
+    const size_t nb = fnum::sa_tc_bytes(ne, bk.K);
+    if ((s = P->alloc(&planes, nb / 2)) || (s = P->alloc(&mb, 1)) || (s = P->upload(&rot, rv))) goto fail;
+    if (fnum::sa_tc_setup(P->satc, D, planes, mb, rot) == cudaSuccess) {
+      P->sa_tc_ok = true;
+      P->info.scratch_bytes += (long long)nb;
+    } else {
+      (void)cudaGetLastError();
+    }
+  }
   {
     cudaError_t e = fnum::launch_twiddles(P->tw, b.N, 0);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -900,6 +926,12 @@ fail:
   return s;
 }
 
+// the synthetic-aperture kernel a plan runs: 1 recurrence kernels, 2 tensor cores
+int sa_variant_of(const fnum_plan* P) {
+  if (P->sa_variant) return P->sa_variant;
+  return P->sa_tc_ok ? 2 : 1;
+}
+
 // the band DFT of d_rf into the plan's spectra; counters[5] collects its error bits
 int plan_dft(fnum_plan* P, const void* rf, int is_double, cudaStream_t st) {
   FNUM_CUDA(cudaMemsetAsync(P->counters + 5, 0, sizeof(unsigned long long), st));
@@ -918,8 +950,12 @@ int plan_beamform(fnum_plan* P, void* image, float* w, float* w2, cudaStream_t s
   FNUM_CUDA(cudaMemsetAsync(P->counters, 0, 5 * sizeof(unsigned long long), st));   // [5] is the DFT's
   const bool plain = (P->flags & FNUM_FLAG_PLAIN_KERNEL) != 0;
   if (P->kind == 1) {
-    cudaError_t e = plain ? fnum::launch_sa_plain(P->sa, (float2*)image, w, w2, st)
-                          : fnum::launch_sa_fused(P->sa, P->grid, (float2*)image, w, w2, st);
+    cudaError_t e;
+    if (plain) e = fnum::launch_sa_plain(P->sa, (float2*)image, w, w2, st);
+    else if (sa_variant_of(P) == 2)
+      e = fnum::launch_sa_tc(P->sa, P->satc, std::min(fnum::sa_tc_grid(P->sa), P->max_grid), (float2*)image, w, w2,
+                             st);
+    else e = fnum::launch_sa_fused(P->sa, P->grid, (float2*)image, w, w2, st);
     return cuda_status(e);
   }
   const fnum::PWDev& D = P->pw;
@@ -981,7 +1017,7 @@ int run_host(fnum_plan* P, const double* rf, size_t rf_count, float* re, float* 
   if (e != cudaSuccess) return cuda_status(e);
   unsigned long long c[8];
   if ((e = cudaMemcpy(c, P->counters, sizeof(c), cudaMemcpyDeviceToHost)) != cudaSuccess) return cuda_status(e);
-  if ((c[2] & fnum::ERR_SEG_OVERFLOW) || (c[5] & fnum::ERR_DFT_TIMEOUT)) return FNUM_ERR_INTERNAL;
+  if ((c[2] & (fnum::ERR_SEG_OVERFLOW | fnum::ERR_TC_TIMEOUT)) || (c[5] & fnum::ERR_DFT_TIMEOUT)) return FNUM_ERR_INTERNAL;
   return FNUM_OK;
 }
 
@@ -1192,7 +1228,8 @@ int fnum_plan_info_get(const fnum_plan* plan, fnum_plan_info* info) {
   info->active_terms = (long long)c[0];
   info->zero_weight_bins = (long long)c[1];
   info->executed_terms = (long long)c[4];
-  info->kernel_variant = plan->kind == 0 ? fnum::pw_variant_of(plan->pw) : 0;
+  info->kernel_variant = plan->kind == 0 ? fnum::pw_variant_of(plan->pw)
+                        : ((plan->flags & FNUM_FLAG_PLAIN_KERNEL) ? 0 : fnum::sa_variant_of(plan));
   info->grid = plan->grid;
   info->blocks_per_sm = 0;
   info->bin_chunk = 0;
@@ -1204,7 +1241,7 @@ int fnum_plan_info_get(const fnum_plan* plan, fnum_plan_info* info) {
                           ? ((plan->pw.tc_tb > 0 && plan->pw.tc_tb < 32) ? plan->pw.tc_tb : 32)
                           : plan->pw.flush_chunks * fnum::KCHUNK;
   }
-  if ((c[2] & fnum::ERR_SEG_OVERFLOW) || (c[5] & fnum::ERR_DFT_TIMEOUT)) return FNUM_ERR_INTERNAL;
+  if ((c[2] & (fnum::ERR_SEG_OVERFLOW | fnum::ERR_TC_TIMEOUT)) || (c[5] & fnum::ERR_DFT_TIMEOUT)) return FNUM_ERR_INTERNAL;
   return FNUM_OK;
 }
 
@@ -1276,7 +1313,7 @@ int fnum_das_pw_sharpness_grad(const fnum_pw_desc* desc, const double* steering_
   }
   unsigned long long c[8];
   FNUM_CUDA(cudaMemcpy(c, P->counters, sizeof(c), cudaMemcpyDeviceToHost));
-  if ((c[2] & fnum::ERR_SEG_OVERFLOW) || (c[5] & fnum::ERR_DFT_TIMEOUT)) return FNUM_ERR_INTERNAL;
+  if ((c[2] & (fnum::ERR_SEG_OVERFLOW | fnum::ERR_TC_TIMEOUT)) || (c[5] & fnum::ERR_DFT_TIMEOUT)) return FNUM_ERR_INTERNAL;
   return FNUM_OK;
 }
 
@@ -1329,7 +1366,12 @@ int fnum_host_cache_info(int saft, long long* plans_created, int* plans_cached) 
 // ---------------------------------------------------------------------------
 int fnum_plan_set_kernel_variant(fnum_plan* plan, int variant) {
   if (!plan) return FNUM_ERR_ARGUMENT;
-  if (plan->kind != 0) return variant == 0 ? FNUM_OK : FNUM_ERR_ARGUMENT;  // one synthetic-aperture variant
+  if (plan->kind != 0) {  // synthetic aperture: 1 recurrence kernels, 2 tensor cores
+    if (variant < 0 || variant > 2 || (variant == 2 && !plan->sa_tc_ok)) return FNUM_ERR_ARGUMENT;
+    if ((plan->flags & FNUM_FLAG_PLAIN_KERNEL) && variant != 0) return FNUM_ERR_ARGUMENT;
+    plan->sa_variant = variant;
+    return FNUM_OK;
+  }
   if (variant < 0 || variant > fnum::pw_variant_count()) return FNUM_ERR_ARGUMENT;
   if (variant == fnum::TC_VARIANT && !plan->pw.tc_B) return FNUM_ERR_ARGUMENT;
   if (plan->pw.m_sem) return variant == 0 ? FNUM_OK : FNUM_ERR_ARGUMENT;     // one per-term kernel
@@ -1339,14 +1381,63 @@ int fnum_plan_set_kernel_variant(fnum_plan* plan, int variant) {
   return FNUM_OK;
 }
 
-int fnum_plan_autotune(fnum_plan* plan, const void* d_rf, int rf_is_double, int* variant, float* ms) {
-  if (!plan || !d_rf) return FNUM_ERR_ARGUMENT;
-  FNUM_CUDA(cudaSetDevice(plan->device));
-  if (plan->kind != 0) {  // the synthetic-aperture kernel has one variant
+// synthetic aperture: times the recurrence kernels (1) and, when the plan has them, the
+// tensor cores (2) on the plan's spectra and keeps the faster
+int autotune_sa(fnum_plan* plan, const void* d_rf, int rf_is_double, int* variant, float* ms) {
+  const int v0 = plan->sa_variant;
+  if (plan->flags & FNUM_FLAG_PLAIN_KERNEL) {
     if (variant) *variant = 0;
     if (ms) *ms = 0.0f;
     return FNUM_OK;
   }
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  float2* img = nullptr;
+  float best = 3.0e38f;
+  int best_v = 1, s = FNUM_OK;
+  const size_t n_img = (size_t)plan->sa.nx * plan->sa.nz;
+  cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) e = cudaMalloc(&img, n_img * sizeof(float2));
+  if (e != cudaSuccess) s = cuda_status(e);
+  if (!s) s = plan_dft(plan, d_rf, rf_is_double, st);
+  for (int v = 1; v <= (plan->sa_tc_ok ? 2 : 1) && !s; ++v) {
+    plan->sa_variant = v;
+    if ((s = plan_beamform(plan, img, nullptr, nullptr, st))) break;
+    float t = 0.0f;
+    cudaError_t e2 = cudaEventRecord(e0, st);
+    for (int r = 0; r < 2 && e2 == cudaSuccess && !s; ++r) s = plan_beamform(plan, img, nullptr, nullptr, st);
+    if (s) break;
+    if (e2 == cudaSuccess) e2 = cudaEventRecord(e1, st);
+    if (e2 == cudaSuccess) e2 = cudaEventSynchronize(e1);
+    if (e2 == cudaSuccess) e2 = cudaEventElapsedTime(&t, e0, e1);
+    if (e2 != cudaSuccess) {
+      s = cuda_status(e2);
+      break;
+    }
+    if (t < best) {
+      best = t;
+      best_v = v;
+    }
+  }
+  plan->sa_variant = s ? v0 : best_v;
+  if (!s) {
+    if (variant) *variant = best_v;
+    if (ms) *ms = 0.5f * best;
+  }
+  if (img) cudaFree(img);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  (void)cudaGetLastError();
+  return s;
+}
+
+int fnum_plan_autotune(fnum_plan* plan, const void* d_rf, int rf_is_double, int* variant, float* ms) {
+  if (!plan || !d_rf) return FNUM_ERR_ARGUMENT;
+  FNUM_CUDA(cudaSetDevice(plan->device));
+  if (plan->kind != 0) return autotune_sa(plan, d_rf, rf_is_double, variant, ms);
   cudaStream_t st = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   float2* img = nullptr;

@@ -103,6 +103,7 @@ struct SADev {
   int seg_cap;
   int flush_chunks;
   float scale;
+  dfl t0N;                          // time offset index_t0 / N in cycles per bin
   const dfl* col_u; const dfl* col_p; const dfl* col_m; const int* col_emid;
   const dfl* row_u2; const dfl* row_p;
   const dfl* el_u; const dfl* el_m; const dfl* el_lb; const dfl* el_ub;
@@ -136,6 +137,7 @@ struct PWBatchDev {
 // error bits in counters[2] (beamformers) and counters[5] (band DFT)
 constexpr unsigned long long ERR_SEG_OVERFLOW = 1ull;
 constexpr unsigned long long ERR_DFT_TIMEOUT = 2ull;   // a wait of the tensor-core DFT gave up
+constexpr unsigned long long ERR_TC_TIMEOUT = 4ull;    // a wait of the tensor-core SAFT kernel gave up
 
 // Band DFT on the tensor cores (fnum_dft_tc.cu): RF lines split into fp16 hi/lo
 // planes a [2][nsig][Kp], twiddle planes b [2][Np][Kp], per-line scale; the TMA
@@ -157,6 +159,23 @@ cudaError_t dft_tc_setup(DftTc& d, int nsig, int nt, int N, int k_lb, int K, con
 // ERR_DFT_TIMEOUT is or-ed into *err if a wait gave up
 cudaError_t dft_tc_run(const DftTc& d, const void* rf, int is_double, float2* X, int lo_n, long long s_hi,
                        long long s_lo, long long s_k, unsigned long long* err, cudaStream_t s);
+
+// Synthetic-aperture beamformer on the tensor cores (fnum_sa_tc.cu): the spectra as
+// fp16 hi/lo planes [bin][2 nep][2 nep] in real form, their TMA maps, the scale word
+// and the time-offset phasors e^{2 pi i k t0 / N} of the band.
+struct SaTc {
+  CUtensorMap tm[2];   // hi, lo (64-byte aligned)
+  void* planes;
+  unsigned* maxbits;
+  const float2* rot;
+  int nep;             // elements rounded up to a multiple of 4
+};
+bool sa_tc_supported(const SADev& d);          // up to 128 elements, accumulating normalisations
+size_t sa_tc_bytes(int ne, int K);             // bytes of the planes
+cudaError_t sa_tc_setup(SaTc& t, const SADev& d, void* planes, unsigned* maxbits, const float2* rot);
+int sa_tc_grid(const SADev& d);                // one block per SM (at most one per tile)
+cudaError_t launch_sa_tc(const SADev& d, const SaTc& t, int grid, float2* image, float* wtx, float* wrx,
+                         cudaStream_t s);
 
 // --- launchers (fnum_kernels.cu) -------------------------------------------
 cudaError_t launch_twiddles(float2* tw, int N, cudaStream_t s);

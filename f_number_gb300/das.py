@@ -504,8 +504,9 @@ class _Plan:
         _lib.check(_lib.lib().fnum_plan_set_shape(self._ptr, int(blocks_per_sm), int(bin_chunk)), self._saft)
 
     def set_kernel_variant(self, variant):
-        """Pins the fused kernel's variant (fnum_plan_set_kernel_variant): 0 = by the
-        angle count, 1..9 for a plane-wave plan."""
+        """Pins the kernel variant (fnum_plan_set_kernel_variant): 0 = default; 1..9 for a
+        plane-wave plan; 1 (recurrence kernels) or 2 (tensor cores) for a
+        synthetic-aperture plan."""
         _lib.check(_lib.lib().fnum_plan_set_kernel_variant(self._ptr, int(variant)), self._saft)
 
 

@@ -207,7 +207,8 @@ typedef struct fnum_plan_info {
   long long scratch_bytes;         /* device scratch the plan owns */
   double scale;                    /* 2 / N_dft */
   long long executed_terms;        /* recurrence steps the fused kernel ran (>= active_terms), last execute */
-  int kernel_variant;              /* PW fused kernel variant (1..9, see fnum_plan_autotune); 0 for SA */
+  int kernel_variant;              /* PW: fused kernel variant (1..9, see fnum_plan_autotune); SA: 1 recurrence
+                                      kernels, 2 tensor cores; 0 for FNUM_FLAG_PLAIN_KERNEL plans */
   int grid;                        /* blocks of the fused kernel's launch */
   int blocks_per_sm;               /* PW: resident blocks per SM of that launch (launch shape) */
   int bin_chunk;                   /* PW: bins between exact phase re-anchorings (tensor cores 32 or 16;
@@ -279,14 +280,17 @@ int fnum_das_pw_noalloc(const fnum_pw_desc* desc, const double* steering_angles,
    angles on) at full occupancy, and keeps the fastest
    for the plan's later executes.  It allocates a temporary image and runs on
    a private stream (not capturable).  variant / ms (the chosen variant's
-   beamform time) may be NULL.  A synthetic-aperture plan has one variant:
-   the call returns variant 0. */
+   beamform time) may be NULL.  A synthetic-aperture plan times its two
+   variants (1: the per-pair recurrence kernels, 2: the tensor-core kernel, which
+   needs up to 128 elements and a normalisation that accumulates, and is the
+   default when available); a FNUM_FLAG_PLAIN_KERNEL plan returns variant 0. */
 int fnum_plan_autotune(fnum_plan* plan, const void* d_rf, int rf_is_double, int* variant, float* ms);
 /* fnum_plan_set_kernel_variant: pins the fused-kernel variant of a plane-wave
    plan (0 = by the angle count, 1..9 as above), e.g. one an earlier
    fnum_plan_autotune chose.  Every variant gives the same images up to the
-   rounding of the per-pass sums.  A synthetic-aperture plan or a plan with
-   FNUM_FLAG_M_SEMANTICS accepts only 0. */
+   rounding of the per-pass sums.  A synthetic-aperture plan accepts 0 (default),
+   1 and 2 (when available); a plan with FNUM_FLAG_M_SEMANTICS or
+   FNUM_FLAG_PLAIN_KERNEL accepts only 0. */
 int fnum_plan_set_kernel_variant(fnum_plan* plan, int variant);
 /* fnum_plan_set_shape: pins the launch shape of a plane-wave plan's current
    variant: blocks_per_sm (0 = as many as fit) and bin_chunk, the bins between
