@@ -120,6 +120,9 @@ __global__ void __launch_bounds__(256) sa_tc_prep_kernel(const float2* __restric
 // ---------------------------------------------------------------------------
 // the beamformer
 // ---------------------------------------------------------------------------
+constexpr int ST_KMAX = 2048;       // bands up to this many bins get per-bin element ranges
+constexpr int ST_NONE = 1 << 20;    // empty range marker
+
 struct StShared {
   int ktop_tx[ST_M];
   int ktop_rx[ST_M];
@@ -127,20 +130,25 @@ struct StShared {
   float2 red[ST_WARPS / 4][ST_M];   // per element slot: the voxel's sum over the slot's elements
   int ranges[4];
   int tile;
-  int E0, C, kt, nb;
+  int E_lo, E_hi, kt, nb;
   unsigned long long n_active, n_empty;
   uint32_t tmem;
   int abort_flag;
   int tma_cnt[2], mma_cnt[2];   // warps through each stage's item so far
   uint64_t bars[7];   // a_full[2], b_full[2], s_empty[2], d_full
+  // per bin (relative to k_lb): the element range of the tile's apertures, tx and rx
+  int lo[ST_KMAX];
+  int hi[ST_KMAX];
 };
 
 // waits as long as no other thread has given up; records a timeout
 __device__ __forceinline__ bool st_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
                                         unsigned long long* err) {
+  if (mbar_test(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
   for (;;) {
-    if (mbar_test(bar, parity)) return true;
+    // sleep in the barrier (up to 20 us per test) instead of spinning on issue slots
+    if (mbar_test_sleep(bar, parity, 20000u)) return true;
     if (*abort_flag) return false;
     if (global_ns() - t0 > WAIT_NS) {
       *abort_flag = 1;
@@ -150,14 +158,16 @@ __device__ __forceinline__ bool st_wait(uint32_t bar, uint32_t parity, volatile 
   }
 }
 
-// window weight of element e for the aperture (lb, ub) of a voxel at xm (0 outside)
+// window weight of element e of a voxel (0 outside its aperture).  The aperture's
+// elements form the interval [a, b] = [min(i_lb, emid), max(i_ub, emid - 1)]: left of
+// emid from i_lb, right of it up to i_ub.
 template <int WIN>
-__device__ __forceinline__ float st_weight(const SADev& d, int e, int emid, int lb, int ub, float iLl, float iLr,
+__device__ __forceinline__ float st_weight(const SADev& d, int e, int emid, int a, int b, float iLl, float iLr,
                                            int ic, float par, float ipar) {
-  const bool left = e < emid;
-  const bool in = left ? (e >= lb) : (e <= ub);
+  const bool in = e >= a && e <= b;
   if (WIN == 0) return in ? 1.0f : 0.0f;
   if (!in) return 0.0f;
+  const bool left = e < emid;
   const dfl c = d.el_m[e], xm = d.col_m[ic];
   const float dx = fabsf((c.x - xm.x) + (c.y - xm.y));
   return win_t<WIN>(par, ipar, dx * (left ? iLl : iLr));
@@ -184,6 +194,8 @@ sa_tc_kernel(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
   auto b_full = [&](int s) { return bar0 + 8u * (uint32_t)(2 + s); };
   auto s_empty = [&](int s) { return bar0 + 8u * (uint32_t)(4 + s); };
   const uint32_t d_full = bar0 + 48u;
+  const int per_bin = d.K <= ST_KMAX;
+  const int n_bins_tab = per_bin ? d.K : 0;
 
   if (tid == 0) {
     for (int s = 0; s < ST_STAGES; ++s) {
@@ -218,7 +230,7 @@ sa_tc_kernel(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
   const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16);
   const uint32_t row_off = (uint32_t)((vb >> 3) * 1024 + (vb & 7) * 128);
   const uint32_t ch0 = (uint32_t)(((2 * slot) ^ (vb & 7)) << 4), ch1 = (uint32_t)(((2 * slot + 1) ^ (vb & 7)) << 4);
-  // running counts of (bin, chunk) items and of bins, the same in every warp
+  // running counts of (bin, chunk) items and of bins with products, the same in every warp
   uint32_t it = 0, bn = 0;
   unsigned long long n_exec = 0;
 
@@ -237,13 +249,16 @@ sa_tc_kernel(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
     const int i = tx_ * TILE_X + q, j = tz_ * TILE_Z + lane;
     const bool vvalid = (i < d.nx) && (j < d.nz);
     const int ic = min(i, d.nx - 1), jc = min(j, d.nz - 1);
-    const int4* seg = d.seg + ((size_t)blockIdx.x * ST_M + vb) * (size_t)d.seg_cap * SA_SEG_INT4;
+    int4* seg = d.seg + ((size_t)blockIdx.x * ST_M + vb) * (size_t)d.seg_cap * SA_SEG_INT4;
+    const int emid = d.col_emid[ic];
+    for (int kk = tid; kk < n_bins_tab; kk += ST_THREADS) {
+      sh.lo[kk] = ST_NONE;
+      sh.hi[kk] = -1;
+    }
     if (warp < 4) {
       float Wt, Wr;
       unsigned long long na = 0, nm = 0;
-      sh.nseg[vb] = sa_build_segments(d, ic, jc, vvalid, d.seg + ((size_t)blockIdx.x * ST_M + vb) * (size_t)d.seg_cap *
-                                                                       SA_SEG_INT4,
-                                      sh.ktop_tx, sh.ktop_rx, sh.ranges, Wt, Wr, na, nm);
+      sh.nseg[vb] = sa_build_segments(d, ic, jc, vvalid, seg, sh.ktop_tx, sh.ktop_rx, sh.ranges, Wt, Wr, na, nm);
       atomicAdd(&sh.n_active, na);
       atomicAdd(&sh.n_empty, nm);
       if (vvalid) {
@@ -254,49 +269,78 @@ sa_tc_kernel(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
     __syncthreads();
     if (tid == 0) {
       const int lo = min(sh.ranges[0], sh.ranges[2]), hi = max(sh.ranges[1], sh.ranges[3]);
-      int E0 = 0, C = 0, kt = -1;
-      if (lo <= hi) {
-        E0 = lo & ~3;
-        C = (hi - E0) / ST_KC + 1;
-        for (int e = E0; e <= min(hi, d.ne - 1); ++e) kt = max(kt, max(sh.ktop_tx[e], sh.ktop_rx[e]));
-      }
-      sh.E0 = E0;
-      sh.C = C;
+      int kt = -1;
+      if (lo <= hi)
+        for (int e = lo; e <= min(hi, d.ne - 1); ++e) kt = max(kt, max(sh.ktop_tx[e], sh.ktop_rx[e]));
+      sh.E_lo = lo;
+      sh.E_hi = hi;
       sh.kt = kt;
-      sh.nb = (C > 0 && kt >= d.k_lb) ? kt - d.k_lb + 1 : 0;
+      sh.nb = (lo <= hi && kt >= d.k_lb) ? kt - d.k_lb + 1 : 0;
     }
     __syncthreads();
-    const int E0 = sh.E0, C = sh.C, kt = sh.kt, nb = sh.nb;
+    const int E_lo = sh.E_lo, E_hi = sh.E_hi, kt = sh.kt, nb = sh.nb;
+    const int E0 = E_lo & ~7;   // the threads' elements: E0 + 32 c + 8 slot + i
+    const int ns = sh.nseg[vb];
+    // per bin, the element range of the tile's apertures: a reduction over each column's
+    // voxels along their segment lists, then over the four columns
+    if (per_bin && nb > 0 && warp < 4) {
+      int sidx = (ns > 0) ? sa_seg_find(seg, ns, kt) : 0;
+      int nxt = (ns > 0) ? seg[min(sidx + 1, ns)].x : -1;
+      int a = ST_NONE, b = -1;
+      auto rng = [&]() {
+        a = ST_NONE;
+        b = -1;
+        if (ns == 0) return;
+        const int4 cur = seg[sidx];
+        if (cur.w == 0) return;   // an empty aperture: no term
+        a = min(min(code_ilb(cur.y), code_ilb(cur.z)), emid);
+        b = max(max(code_iub(cur.y), code_iub(cur.z)), emid - 1);
+      };
+      rng();
+      for (int k = kt; k >= d.k_lb; --k) {
+        if (k == nxt) {
+          ++sidx;
+          nxt = seg[min(sidx + 1, ns)].x;
+          rng();
+        }
+        const int mn = __reduce_min_sync(0xffffffffu, a), mx = __reduce_max_sync(0xffffffffu, b);
+        if (lane == 0 && mn <= mx) {
+          atomicMin(&sh.lo[k - d.k_lb], mn);
+          atomicMax(&sh.hi[k - d.k_lb], mx);
+        }
+      }
+    }
+    __syncthreads();
     float2 acc = make_float2(0.0f, 0.0f), comp = make_float2(0.0f, 0.0f);
     if (nb > 0) {
-      const int emid = d.col_emid[ic];
       auto u_of = [&](int e) {
         return df_sqrt(df_add(df_sqr(df_sub(d.el_u[min(e, d.ne - 1)], d.col_u[ic])), d.row_u2[jc]));
       };
-      // rho = e^{2 pi i u} of the thread's elements into tensor memory
-      for (int c = 0; c < C; ++c) {
+      // rho = e^{2 pi i u} of the thread's elements into tensor memory, by element pairs
+      // {Re rho_2j, Re rho_2j+1, Im rho_2j, Im rho_2j+1} (the packed recurrence's operands)
+      for (int c = 0; c * ST_KC <= E_hi - E0; ++c) {
         float rv[16];
 #pragma unroll
         for (int k2 = 0; k2 < ST_EPT; ++k2) {
           const float2 r = cis_ku(1, u_of(E0 + ST_KC * c + ST_EPT * slot + k2));
-          rv[2 * k2] = r.x;
-          rv[2 * k2 + 1] = r.y;
+          rv[4 * (k2 >> 1) + (k2 & 1)] = r.x;
+          rv[4 * (k2 >> 1) + 2 + (k2 & 1)] = r.y;
         }
         tmem_st16(tl + (uint32_t)(ST_RHO_COL + 2 * ST_KC * c + 2 * ST_EPT * slot), rv);
       }
       tmem_wait_st();
       // the segment in effect: its apertures, normaliser and (other windows) half-widths
-      const int ns = sh.nseg[vb];
+      // (the next entry is loaded a boundary ahead, so its latency hides behind whole bins)
       int sidx = (ns > 0) ? sa_seg_find(seg, ns, kt) : 0;
-      int nxt_k = (ns > 0) ? seg[min(sidx + 1, ns)].x : -1;
-      int tlb = 0, tub = -1, rlb = 0, rub = -1;
+      int4 nxt = (ns > 0) ? seg[min(sidx + 1, ns)] : make_int4(-1, 0, 0, 0);
+      int ta = 0, tb = -1, ra = 0, rb = -1;
       float nrm = 0.0f, tLl = 0.0f, tLr = 0.0f, rLl = 0.0f, rLr = 0.0f;
-      auto derive = [&]() {
-        const int4 cur = (ns > 0) ? seg[sidx] : make_int4(-1, seg_code(d.ne, -1), seg_code(d.ne, -1), 0);
-        tlb = code_ilb(cur.y);
-        tub = code_iub(cur.y);
-        rlb = code_ilb(cur.z);
-        rub = code_iub(cur.z);
+      auto derive = [&](const int4 cur) {
+        const int tlb = code_ilb(cur.y), tub = code_iub(cur.y), rlb = code_ilb(cur.z), rub = code_iub(cur.z);
+        ta = min(tlb, emid);
+        tb = max(tub, emid - 1);
+        ra = min(rlb, emid);
+        rb = max(rub, emid - 1);
         nrm = __int_as_float(cur.w);
         if (WT != 0 || WR != 0) {
           const dfl xm = d.col_m[ic];
@@ -310,86 +354,137 @@ sa_tc_kernel(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
           }
         }
       };
-      derive();
-      float2 p[ST_CMAX][ST_EPT];
+      derive((ns > 0) ? seg[sidx] : make_int4(-1, seg_code(d.ne, -1), seg_code(d.ne, -1), 0));
+      // phasors by element pairs: pr[c][j] = {Re p_2j, Re p_2j+1}, pm[c][j] = {Im p_2j, Im p_2j+1}
+      float2 pr[ST_CMAX][ST_EPT / 2], pm[ST_CMAX][ST_EPT / 2];
 #pragma unroll
       for (int c = 0; c < ST_CMAX; ++c)
 #pragma unroll
-        for (int k2 = 0; k2 < ST_EPT; ++k2) p[c][k2] = make_float2(0.0f, 0.0f);
-      const uint32_t idesc = idesc_f16(ST_M, 2 * ST_KC * C);
-      const uint32_t box_bytes = (uint32_t)(2 * C * ST_BOX_BYTES);
+        for (int j2 = 0; j2 < ST_EPT / 2; ++j2) pr[c][j2] = pm[c][j2] = make_float2(0.0f, 0.0f);
+      // per chunk: p holds the phasors of the previous bin (else the next use re-anchors)
+      unsigned live = 0u;
       bool ok = true;
       for (int b = 0; b < nb && ok; ++b) {
         const int k = kt - b;
-        if (k == nxt_k) {
+        if (k == nxt.x) {
+          const int4 cur = nxt;
           ++sidx;
-          nxt_k = seg[min(sidx + 1, ns)].x;
-          derive();
+          nxt = seg[min(sidx + 1, ns)];
+          derive(cur);
         }
+        int lo = E_lo, hi = E_hi;
+        if (per_bin) {
+          lo = sh.lo[k - d.k_lb];
+          hi = sh.hi[k - d.k_lb];
+        }
+        if (lo > hi) {   // no aperture in the tile at this bin
+          live = 0u;
+          continue;
+        }
+        // this bin's chunks c_lo..c_hi; transmit rows from E0b (D column 2 (e - E0b))
+        const int E0b = lo & ~7;
+        const int c_lo = (lo - E0) >> 5, c_hi = (hi - E0) >> 5;
+        const int nN = 16 * ((hi - E0b + 8) >> 3);
+        const uint32_t idesc = idesc_f16(ST_M, nN);
+        const int nbox = (nN + ST_BOX_ROWS - 1) / ST_BOX_ROWS;
+        const uint32_t box_bytes = (uint32_t)(2 * nbox * ST_BOX_BYTES);
         const bool anchor = (b % ST_TB) == 0;
+        unsigned nlive = 0u;
+        int n_items = 0;
 #pragma unroll
         for (int c = 0; c < ST_CMAX; ++c) {
-          if (c < C) {
-            const int eb = E0 + ST_KC * c + ST_EPT * slot;
-            if (anchor) {
-#pragma unroll
-              for (int k2 = 0; k2 < ST_EPT; ++k2) p[c][k2] = cis_ku(k, u_of(eb + k2));
-            } else {
-              float rv[16];
-              tmem_ld16_nowait(tl + (uint32_t)(ST_RHO_COL + 2 * ST_KC * c + 2 * ST_EPT * slot), rv);
-              tmem_wait_ld();
-#pragma unroll
-              for (int k2 = 0; k2 < ST_EPT; ++k2) {
-                const float2 o = p[c][k2];
-                const float rr = rv[2 * k2], ri = rv[2 * k2 + 1];
-                p[c][k2] = make_float2(fmaf(o.x, rr, o.y * ri), fmaf(o.y, rr, -o.x * ri));
-              }
-            }
-            uint32_t hi[ST_EPT], lo[ST_EPT];
-#pragma unroll
-            for (int k2 = 0; k2 < ST_EPT; ++k2) {
-              const float w = st_weight<WR>(d, eb + k2, emid, rlb, rub, rLl, rLr, ic, d.wrx_par, ipr);
-              const float br = w * p[c][k2].x, bi = w * p[c][k2].y;
-              const __half2 h = __floats2half2_rn(br, bi);
-              const float2 f = __half22float2(h);
-              hi[k2] = h2u(h);
-              lo[k2] = h2u(__floats2half2_rn(br - f.x, bi - f.y));
-            }
+          if (c >= c_lo && c <= c_hi) {
+            const int g0 = E0 + ST_KC * c;
+            const int s_lo = max(0, (lo - g0) >> 3), s_hi = min(ST_KC / ST_EPT - 1, (hi - g0) >> 3);
+            const bool mine = slot >= s_lo && slot <= s_hi;
+            const int eb = g0 + ST_EPT * slot;
+            const bool exact = anchor || !(live & (1u << c));
             const int st = (int)(it & 1u);
             const uint32_t ph = (it >> 1) & 1u;
-            // the stage is free once the products of the item two back have read it
-            ok = __all_sync(0xffffffffu, st_wait(s_empty(st), ph ^ 1u, abort_flag, err));
-            if (!ok) break;
-            if (lane == 0) {
-              // the first warp through issues the item's B tile, the last one resets the count
-              const int o = atomicAdd(&sh.tma_cnt[st], 1);
-              if (o == 0) {
-                const uint32_t bh = base + (uint32_t)(st * ST_STAGE + 2 * ST_A_PLANE);
-                const uint32_t bl = bh + ST_B_PLANE;
-                mbar_expect_tx(b_full(st), box_bytes);
-                const int x = 2 * E0 + 2 * ST_KC * c, z = k - d.k_lb;
-                for (int jj = 0; jj < C; ++jj) {
-                  const int y = 2 * E0 + ST_BOX_ROWS * jj;
-                  tma_load_3d(bh + (uint32_t)(jj * ST_BOX_BYTES), &tm_hi, x, y, z, b_full(st));
-                  tma_load_3d(bl + (uint32_t)(jj * ST_BOX_BYTES), &tm_lo, x, y, z, b_full(st));
-                }
-              } else if (o == ST_WARPS - 1) {
-                sh.tma_cnt[st] = 0;
-              }
-            }
             unsigned char* ahi = gbase + st * ST_STAGE;
             unsigned char* alo = ahi + ST_A_PLANE;
-            *reinterpret_cast<uint4*>(ahi + row_off + ch0) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-            *reinterpret_cast<uint4*>(ahi + row_off + ch1) = make_uint4(hi[4], hi[5], hi[6], hi[7]);
-            *reinterpret_cast<uint4*>(alo + row_off + ch0) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
-            *reinterpret_cast<uint4*>(alo + row_off + ch1) = make_uint4(lo[4], lo[5], lo[6], lo[7]);
-            fence_proxy_async_smem();
+            // two halves of 4 elements: phasors, A values, then (once the stage is free) the stores
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              uint32_t hq[4], lq[4];
+              if (mine) {
+                if (exact) {
+#pragma unroll
+                  for (int jj = 0; jj < 2; ++jj) {
+                    const int j2 = 2 * h + jj;
+                    const float2 z0 = cis_ku(k, u_of(eb + 2 * j2)), z1 = cis_ku(k, u_of(eb + 2 * j2 + 1));
+                    pr[c][j2] = make_float2(z0.x, z1.x);
+                    pm[c][j2] = make_float2(z0.y, z1.y);
+                  }
+                } else {
+                  // p <- p conj(rho), two elements per packed FP32 instruction
+                  float rv[8];
+                  tmem_ld8_nowait(tl + (uint32_t)(ST_RHO_COL + 2 * ST_KC * c + 2 * ST_EPT * slot + 8 * h), rv);
+                  tmem_wait_ld();
+#pragma unroll
+                  for (int jj = 0; jj < 2; ++jj) {
+                    const int j2 = 2 * h + jj;
+                    const float2 rr = make_float2(rv[4 * jj], rv[4 * jj + 1]);
+                    const float2 ri = make_float2(rv[4 * jj + 2], rv[4 * jj + 3]);
+                    const float2 a = pr[c][j2], m = pm[c][j2];
+                    const float2 t = __fmul2_rn(a, ri);
+                    pr[c][j2] = __ffma2_rn(m, ri, __fmul2_rn(a, rr));
+                    pm[c][j2] = __ffma2_rn(m, rr, make_float2(-t.x, -t.y));
+                  }
+                }
+#pragma unroll
+                for (int kq = 0; kq < 4; ++kq) {
+                  const int k2 = 4 * h + kq;
+                  const float w = st_weight<WR>(d, eb + k2, emid, ra, rb, rLl, rLr, ic, d.wrx_par, ipr);
+                  const float px = (k2 & 1) ? pr[c][k2 >> 1].y : pr[c][k2 >> 1].x;
+                  const float py = (k2 & 1) ? pm[c][k2 >> 1].y : pm[c][k2 >> 1].x;
+                  const float br = w * px, bi = w * py;
+                  const __half2 hh = __floats2half2_rn(br, bi);
+                  const float2 f = __half22float2(hh);
+                  hq[kq] = h2u(hh);
+                  lq[kq] = h2u(__floats2half2_rn(br - f.x, bi - f.y));
+                }
+              }
+              if (h == 0) {
+                // the stage is free once the products of the item two back have read it
+                ok = __all_sync(0xffffffffu, st_wait(s_empty(st), ph ^ 1u, abort_flag, err));
+                if (!ok) break;
+                if (lane == 0) {
+                  // the first warp through issues the item's B tiles, the last one resets the count
+                  const int o = atomicAdd(&sh.tma_cnt[st], 1);
+                  if (o == 0) {
+                    const uint32_t bh = base + (uint32_t)(st * ST_STAGE + 2 * ST_A_PLANE);
+                    const uint32_t bl = bh + ST_B_PLANE;
+                    mbar_expect_tx(b_full(st), box_bytes);
+                    const int x = 2 * g0, z = k - d.k_lb;
+                    for (int jj = 0; jj < nbox; ++jj) {
+                      const int y = 2 * E0b + ST_BOX_ROWS * jj;
+                      tma_load_3d(bh + (uint32_t)(jj * ST_BOX_BYTES), &tm_hi, x, y, z, b_full(st));
+                      tma_load_3d(bl + (uint32_t)(jj * ST_BOX_BYTES), &tm_lo, x, y, z, b_full(st));
+                    }
+                  } else if (o == ST_WARPS - 1) {
+                    sh.tma_cnt[st] = 0;
+                  }
+                }
+              }
+              if (mine) {
+                const uint32_t chh = h ? ch1 : ch0;
+                *reinterpret_cast<uint4*>(ahi + row_off + chh) = make_uint4(hq[0], hq[1], hq[2], hq[3]);
+                *reinterpret_cast<uint4*>(alo + row_off + chh) = make_uint4(lq[0], lq[1], lq[2], lq[3]);
+              }
+            }
+            if (!ok) break;
+            if (mine) {
+              nlive |= 1u << c;
+              fence_proxy_async_smem();
+            }
             fence_before_sync();
             __syncwarp();
             if (lane == 0) {
               mbar_arrive(a_full(st));
-              // the last warp in issues the item's products (all A rows are written, and for
-              // the bin's first chunk every warp has read the previous bin's D)
+              // the last warp in issues the item's products for the chunk's live k-steps (all A
+              // rows are written, and for the bin's first chunk every warp has read the previous
+              // bin's D)
               const int o = atomicAdd(&sh.mma_cnt[st], 1);
               if (o == ST_WARPS - 1) {
                 sh.mma_cnt[st] = 0;
@@ -398,50 +493,59 @@ sa_tc_kernel(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
                   const uint32_t ah = base + (uint32_t)(st * ST_STAGE);
                   const uint32_t al = ah + ST_A_PLANE, bh = ah + 2 * ST_A_PLANE, bl = bh + ST_B_PLANE;
                   // the small cross products first, so that only the hi.hi steps round a full-size sum
-#pragma unroll
-                  for (int kk = 0; kk < 4; ++kk) {
+                  for (int kk = s_lo; kk <= s_hi; ++kk) {
                     const uint32_t off = (uint32_t)kk * 32u;
-                    mma_f16(tmem, smem_desc(ah + off), smem_desc(bl + off), idesc, (c != 0 || kk != 0) ? 1u : 0u);
+                    mma_f16(tmem, smem_desc(ah + off), smem_desc(bl + off), idesc,
+                            (c != c_lo || kk != s_lo) ? 1u : 0u);
                     mma_f16(tmem, smem_desc(al + off), smem_desc(bh + off), idesc, 1u);
                   }
-#pragma unroll
-                  for (int kk = 0; kk < 4; ++kk) {
+                  for (int kk = s_lo; kk <= s_hi; ++kk) {
                     const uint32_t off = (uint32_t)kk * 32u;
                     mma_f16(tmem, smem_desc(ah + off), smem_desc(bh + off), idesc, 1u);
                   }
                   mma_commit(s_empty(st));
-                  if (c == C - 1) mma_commit(d_full);
+                  if (c == c_hi) mma_commit(d_full);
                 }
+                n_exec += (unsigned long long)ST_M * (ST_EPT * (s_hi - s_lo + 1)) * (nN / 2);
               }
             }
             __syncwarp();
             ++it;
+            ++n_items;
           }
         }
+        live = nlive;
         if (!ok) break;
         // the bin's Y: dot with the transmit phasors.  d_full is committed by the thread that
         // issued the bin's last products; the item before it (another issuer, other stage)
         // is complete when its stage is released (items on one stage complete in turn)
         ok = __all_sync(0xffffffffu, st_wait(d_full, bn & 1u, abort_flag, err) &&
-                                         (C < 2 || st_wait(s_empty((int)(it & 1u)), ((it - 2) >> 1) & 1u, abort_flag,
-                                                           err)));
+                                         (n_items < 2 || st_wait(s_empty((int)(it & 1u)), ((it - 2) >> 1) & 1u,
+                                                                 abort_flag, err)));
         if (!ok) break;
         fence_after_sync();
         float2 part = make_float2(0.0f, 0.0f);
 #pragma unroll
         for (int c = 0; c < ST_CMAX; ++c) {
-          if (c < C) {
-            float yv[16];
-            tmem_ld16_nowait(tl + (uint32_t)(2 * ST_KC * c + 2 * ST_EPT * slot), yv);
-            tmem_wait_ld();
+          if (nlive & (1u << c)) {
+            const int col = 2 * ST_KC * c + 2 * ST_EPT * slot - 2 * (E0b - E0);
             const int eb = E0 + ST_KC * c + ST_EPT * slot;
 #pragma unroll
-            for (int k2 = 0; k2 < ST_EPT; ++k2) {
-              const float w = st_weight<WT>(d, eb + k2, emid, tlb, tub, tLl, tLr, ic, d.wtx_par, ipt);
-              const float ar = w * p[c][k2].x, ai = w * p[c][k2].y;
-              const float yr = yv[2 * k2], yi = yv[2 * k2 + 1];
-              part.x = fmaf(ar, yr, fmaf(-ai, yi, part.x));
-              part.y = fmaf(ar, yi, fmaf(ai, yr, part.y));
+            for (int h = 0; h < 2; ++h) {
+              float yv[8];
+              tmem_ld8_nowait(tl + (uint32_t)(col + 8 * h), yv);
+              tmem_wait_ld();
+#pragma unroll
+              for (int kq = 0; kq < 4; ++kq) {
+                const int k2 = 4 * h + kq;
+                const float w = st_weight<WT>(d, eb + k2, emid, ta, tb, tLl, tLr, ic, d.wtx_par, ipt);
+                const float px = (k2 & 1) ? pr[c][k2 >> 1].y : pr[c][k2 >> 1].x;
+                const float py = (k2 & 1) ? pm[c][k2 >> 1].y : pm[c][k2 >> 1].x;
+                const float ar = w * px, ai = w * py;
+                const float yr = yv[2 * kq], yi = yv[2 * kq + 1];
+                part.x = fmaf(ar, yr, fmaf(-ai, yi, part.x));
+                part.y = fmaf(ar, yi, fmaf(ai, yr, part.y));
+              }
             }
           }
         }
@@ -454,7 +558,6 @@ sa_tc_kernel(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
         comp.y = (sy - acc.y) - yy;
         acc.y = sy;
       }
-      if (tid == 0) n_exec += (unsigned long long)ST_M * (ST_KC * C) * (ST_KC * C) * nb;
     }
     sh.red[slot][vb] = acc;
     fence_before_sync();
@@ -472,10 +575,10 @@ sa_tc_kernel(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ 
       image[(size_t)ic * d.nz + jc] = make_float2(sx * f, sy * f);
     }
   }
+  atomicAdd(&d.counters[4], n_exec);
   if (tid == 0) {
     atomicAdd(&d.counters[0], sh.n_active);
     atomicAdd(&d.counters[1], sh.n_empty);
-    atomicAdd(&d.counters[4], n_exec);
     // after a timeout, give the copies and products in flight time to land before the
     // tensor memory is freed (they take microseconds)
     if (*abort_flag) {
