@@ -213,18 +213,22 @@ dft_tc_gemm_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_cons
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t st = base + (uint32_t)s * DT_STAGE_BYTES;
         const uint32_t acc = tmem + (uint32_t)(j * DT_BN);
+        // descriptors once per stage; a k-step of 16 fp16 (32 bytes) adds 2 to the
+        // start-address field
+        const uint64_t dah = smem_desc(st), dal = smem_desc(st + DT_TILE_BYTES);
+        const uint64_t dbh = smem_desc(st + 2 * DT_TILE_BYTES), dbl = smem_desc(st + 3 * DT_TILE_BYTES);
         // the small cross products first, so that only the four hi.hi steps round a
         // full-size accumulator
 #pragma unroll
         for (int kk = 0; kk < DT_BK / 16; ++kk) {
-          const uint32_t off = (uint32_t)kk * 32u;   // 16 fp16 along K
-          tc_mma_f16(acc, smem_desc(st + off), smem_desc(st + 3 * DT_TILE_BYTES + off), kk != 0);          // hi.lo
-          tc_mma_f16(acc, smem_desc(st + DT_TILE_BYTES + off), smem_desc(st + 2 * DT_TILE_BYTES + off), 1u);  // lo.hi
+          const uint64_t o = 2ull * (uint64_t)kk;
+          tc_mma_f16(acc, dah + o, dbl + o, kk != 0);   // hi.lo
+          tc_mma_f16(acc, dal + o, dbh + o, 1u);        // lo.hi
         }
 #pragma unroll
         for (int kk = 0; kk < DT_BK / 16; ++kk) {
-          const uint32_t off = (uint32_t)kk * 32u;
-          tc_mma_f16(acc, smem_desc(st + off), smem_desc(st + 2 * DT_TILE_BYTES + off), 1u);               // hi.hi
+          const uint64_t o = 2ull * (uint64_t)kk;
+          tc_mma_f16(acc, dah + o, dbh + o, 1u);        // hi.hi
         }
         tc_commit(empty(s));   // the stage is free once these products have read it
         tc_commit(accf(j));    // and the accumulator holds the stage's sums
