@@ -866,7 +866,7 @@ __global__ void __launch_bounds__(256) tc_prep_kernel(const PWDev d, int n_ap) {
 
 // Shared memory of pw_tc_kernel's tile body.
 struct TcShared {
-  float4 apt[TC_WARPS][TC_TT][16];   // {-, 1/L_left, 1/L_right, 1/W} per bin, voxel
+  float4 apt[TC_WARPS][TC_TT][16];   // {segment index (int bits), 1/L_left, 1/L_right, 1/W} per bin, voxel
   int e_range[2];
   int s_nseg[TC_WARPS * 16];
   // table builders' state (entry in effect, next segment entry, its index) and the
@@ -1040,6 +1040,7 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
           if (bnseg > 0) {
             bs = seg_find1(bseg, bnseg, kt);
             bent = entry_of(bseg[bs]);
+            bent.x = __int_as_float(bs);
             bnext = bseg[min(bs + 1, bnseg)];
           }
           b_ent[bv] = bent;
@@ -1047,6 +1048,9 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
           b_idx[bv] = bs;
         }
         const uint4* Bpe = Bp + (size_t)(e0 >> 3) * 96 + lane;
+        // the pairs' weights of the segment in effect, recomputed when a voxel enters a new segment
+        float bw[2][TC_KS][2];
+        int wid[2] = {-1, -1};
         for (int kc_hi = kt; kc_hi >= d.k_lb; kc_hi -= tb) {
           const int kc_lo = max(d.k_lb, kc_hi - (tb - 1));
           // receive phasors re-anchored exactly at the chunk's first bin
@@ -1079,6 +1083,7 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
                 if (k == bnext.x) {
                   bent = entry_of(bnext);
                   ++bs;
+                  bent.x = __int_as_float(bs);
                   bnext = bseg[min(bs + 1, bnseg)];
                 }
                 apt[warp][kt_hi - k][lane] = bent;
@@ -1092,6 +1097,21 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
               float4 en[2];
               en[0] = apt[warp][kt_hi - k][g];
               en[1] = apt[warp][kt_hi - k][g + 8];
+#pragma unroll
+              for (int V = 0; V < 2; ++V) {
+                const int sid = __float_as_int(en[V].x);
+                if (sid != wid[V]) {
+                  wid[V] = sid;
+#pragma unroll
+                  for (int s = 0; s < TC_KS; ++s)
+#pragma unroll
+                    for (int i = 0; i < 2; ++i) {
+                      const float2 dlr = s_dx[2 * TC_KS * V + 2 * s + i][tid];
+                      const float u = fmaf(dlr.x, en[V].y, dlr.y * en[V].z);
+                      bw[V][s][i] = (u < 1.0f) ? win_t<WIN>(d.window_par, inv_par, u) * en[V].w : 0.0f;
+                    }
+                }
+              }
               // H <- H t (derivative chains: Q <- (Q + P) t, P <- P t)
 #pragma unroll
               for (int j = 0; j < 3; ++j)
@@ -1122,15 +1142,8 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
                 float2 rre[2], rim[2];
 #pragma unroll
                 for (int V = 0; V < 2; ++V) {
-                  float b[2];
-#pragma unroll
-                  for (int i = 0; i < 2; ++i) {
-                    const float2 dlr = s_dx[2 * TC_KS * V + 2 * s + i][tid];
-                    const float u = fmaf(dlr.x, en[V].y, dlr.y * en[V].z);
-                    b[i] = (u < 1.0f) ? win_t<WIN>(d.window_par, inv_par, u) * en[V].w : 0.0f;
-                  }
                   // R = b r^k and r^k <- r^k conj(r), two elements per packed FP32 instruction
-                  const float2 bb = make_float2(b[0], b[1]);
+                  const float2 bb = make_float2(bw[V][s][0], bw[V][s][1]);
                   const float2 Pr = pr[V][s], Pi = pim[V][s];
                   rre[V] = __fmul2_rn(bb, Pr);
                   rim[V] = __fmul2_rn(bb, Pi);
