@@ -259,9 +259,8 @@ int fnum_host_cache_info(int saft, long long* plans_created, int* plans_cached);
                else n_angles), scaled by 2 / N_dft; d_weights [n_x][n_z] or NULL
      flags     0 or FNUM_FLAG_COMPOUND
    The first call on a device looks up the array's device address (once per
-   device, with that device current): make that first call before any stream
-   capture, and do not reset the device (cudaDeviceReset, MATLAB's
-   reset(gpuDevice)) between calls, since the address is kept.  Arguments are
+   device, with that device current) and keeps it: do not reset the device
+   (cudaDeviceReset, MATLAB's reset(gpuDevice)) between calls.  Arguments are
    checked as fnum_das_pw checks them, with the same status codes.  Problems whose tables, spectra and one block of aperture segments
    do not fit return FNUM_ERR_NOALLOC_TOO_LARGE; larger ones run with as many
    resident blocks as fit.  All calls share the array and it keeps the last
