@@ -170,7 +170,7 @@ def accuracy_of(wl, win, fn, img, n_random=192, n_bright=64):
 
 
 def measured_peaks():
-    """The machine's measured HBM and bf16 peaks (MEASURED_PEAKS.json beside this file), or {}."""
+    """Measured HBM and bf16 peaks of the GPU (MEASURED_PEAKS.json beside this file), or {}."""
     try:
         with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
             return json.load(f)

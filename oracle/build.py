@@ -6,8 +6,8 @@ TEST INFRASTRUCTURE ONLY.
 * oracle/_ref/ref_kernels.fatbin: the reference's own CUDA kernels compiled
   from their sources in the reference checkout's +cuda directory (device code
   for sm_103a only; built where the reference is mounted, then shipped with the
-  tree).  The checkout is $FNUM_REFERENCE_ROOT, or ``--reference DIR``; its
-  default is where this build environment mounts it.
+  tree).  The checkout is $FNUM_REFERENCE_ROOT, or ``--reference DIR``, by
+  default /root/reference.
 * oracle/_ref/libref_harness.so: the project-written host driver that runs
   those kernels with the MEX host sequence (nvcc; built wherever the fatbin
   and a CUDA toolkit are present).
