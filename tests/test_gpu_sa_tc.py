@@ -160,3 +160,15 @@ def test_variant_api(gpu):
             plan.set_kernel_variant(2)
     finally:
         plan.close()
+
+
+def test_tc_long_band_tile_ranges(gpu):
+    """More than 2048 band bins: the kernel uses each tile's element range for every bin
+    (no per-bin table) and must give the same image."""
+    arr, rf, px, pz = case(8, seed=21, nx=5, nz=4, n_t=4700)
+    img2, _, _, info = run_plan(arr, rf, px, pz, 2, fb=(0.2e6, 19.9e6))
+    assert info["kernel_variant"] == 2 and info["n_bins"] > 2048
+    img1, _, _, _ = run_plan(arr, rf, px, pz, 1, fb=(0.2e6, 19.9e6))
+    ref, _, _ = oracle(arr, rf, px, pz, fb=(0.2e6, 19.9e6))
+    assert rel_l2(img2, ref) < TOL_L2
+    assert rel_l2(img2, img1) < TOL_VAR
