@@ -23,19 +23,22 @@
 // Kernel (persistent, one CTA per SM, tiles from a deepest-first counter), 16 warps.
 // Warp w serves the TMEM lane quadrant w mod 4 (one tile column, 32 voxels, a voxel
 // per lane) and the element slot w / 4 (elements 8s .. 8s+7 of every 32-element
-// chunk).  Per bin and chunk the warps advance their phasors p = e^{2 pi i k u} by
-// p <- p conj(rho) (rho = e^{2 pi i u} kept in tensor memory, columns 256-511;
-// exact re-anchoring every 32 bins) and write their A rows (fp16 hi/lo, 128-byte
-// swizzle) into a two-stage shared-memory ring.  The first warp through a stage
-// issues the item's B tiles (TMA, a 3-D map over [bin][row][column]); the last one
-// in issues its tcgen05.mma (M = 128, N = 64 x chunks, K = 16: hi.lo and lo.hi
-// first, then hi.hi) into the single D accumulator and commits the stage and, after
-// the bin's last chunk, D.  Once D is complete every thread reads its 16 columns and
-// adds n_k sum_t w_tx p_t Y_t to its voxel (compensated sum); the next bin's first
-// products are only issued after every warp has passed that point, so D is free.
-// Every wait on an mbarrier gives up after two seconds: the CTA then records
-// ERR_TC_TIMEOUT, gives its copies and products in flight time to land, frees its
-// tensor memory and returns.
+// chunk, one mma k-step).  Per tile the elements span the union of its voxels'
+// apertures; per bin only the chunks and k-steps that bin's apertures touch run
+// (the per-bin ranges come from a warp reduction along each column's segment lists),
+// with N = 16 ceil(transmit elements / 8).  Per bin and chunk the warps advance their
+// phasors p = e^{2 pi i k u} by p <- p conj(rho) in packed FP32x2 (rho = e^{2 pi i u}
+// kept in tensor memory, columns 256-511; exact re-anchoring every 32 bins and when a
+// chunk comes back into range) and write their A rows (fp16 hi/lo, 128-byte swizzle)
+// into a two-stage shared-memory ring.  The first warp through a stage issues the
+// item's B tiles (TMA, a 3-D map over [bin][row][column]); the last one in issues its
+// tcgen05.mma (M = 128, K = 16 per k-step: hi.lo and lo.hi first, then hi.hi) into
+// the single D accumulator and commits the stage and, after the bin's last chunk, D.
+// Once D is complete every thread reads its columns and adds n_k sum_t w_tx p_t Y_t
+// to its voxel (compensated sum); the next bin's first products are only issued
+// after every warp has passed that point, so D is free.  Waits sleep in the mbarrier
+// and give up after two seconds: the CTA then records ERR_TC_TIMEOUT, gives its
+// copies and products in flight time to land, frees its tensor memory and returns.
 #include <cuda.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
