@@ -454,6 +454,8 @@ struct fnum_plan {
   float2* adj_gX = nullptr;
   double* adj_sums = nullptr;
   double* adj_acc = nullptr;   // FP64 sums of the voxel slices, 2 per spectrum entry
+  float4* adj_rx = nullptr;    // receive delays and steps of the adjoint (PWDev::rx_tab)
+  bool adj_rx_tried = false;
   unsigned* adj_gmax = nullptr;  // fp16 scale inputs of the adjoint: max |G|, max 1/W
   bool adj_invw_ready = false;
   // band DFT on the tensor cores: fp16 hi/lo operand planes, per-line scales, TMA maps
@@ -1860,6 +1862,12 @@ int adjoint_buffers(fnum_plan* plan, cudaStream_t st) {
         (s = plan->alloc(&plan->adj_gX, nspec)) || (s = plan->alloc(&plan->adj_sums, 4)) ||
         (s = plan->alloc(&plan->adj_acc, 2 * nspec)) || (s = plan->alloc(&plan->adj_gmax, 2)))
       return s;
+  }
+  // the adjoint's per-(voxel, element) receive table (16 bytes a pair) is optional: without
+  // the memory the kernel forms the same values itself
+  if (!plan->adj_rx_tried) {
+    plan->adj_rx_tried = true;
+    if (plan->alloc(&plan->adj_rx, (size_t)nvox * D.ne) == FNUM_OK) plan->pw.rx_tab = plan->adj_rx;
   }
   if (!plan->adj_invw_ready) {
     FNUM_CUDA(fnum::launch_pw_invw(D, plan->adj_invw, st));

@@ -93,6 +93,9 @@ struct PWDev {
   double m_c, m_fs, m_t0, m_pitch, m_width, m_M;
   float2* m_sig;        // [nz][K] focused spectra of the last column (signal output)
   int* m_sig_flag;      // [nz] 1 where the voxel has an active bin
+  // adjoint: {u_rx (double-float), e^{2 pi i u_rx}} per (voxel, element), voxel-major;
+  // null when the table could not be allocated (the adjoint then forms them itself)
+  float4* rx_tab;
 };
 
 struct SADev {

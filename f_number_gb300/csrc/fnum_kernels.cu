@@ -43,6 +43,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <mutex>
+
 namespace fnum {
 
 
@@ -806,6 +808,21 @@ __device__ __forceinline__ void tc_split(float x0, float x1, unsigned& hi, unsig
   lo = *reinterpret_cast<const unsigned*>(&l);
 }
 
+// the same split with the residual from sm_100's mixed-precision FMA: lo = x - hi
+// in one instruction per value (fp16 source, fp32 result; x - hi is exact, so the
+// halves are those of tc_split)
+__device__ __forceinline__ void tc_split_mx(float x0, float x1, unsigned& hi, unsigned& lo) {
+  asm("{\n\t.reg .b16 h0, h1, m;\n\t.reg .f32 l0, l1;\n\t"
+      "cvt.rn.f16x2.f32 %0, %3, %2;\n\t"
+      "mov.b32 {h0, h1}, %0;\n\t"
+      "mov.b16 m, 0xBC00;\n\t"
+      "fma.rn.f32.f16 l0, h0, m, %2;\n\t"
+      "fma.rn.f32.f16 l1, h1, m, %3;\n\t"
+      "cvt.rn.f16x2.f32 %1, l1, l0;\n\t}"
+      : "=&r"(hi), "=r"(lo)
+      : "f"(x0), "f"(x1));
+}
+
 // D += A B for one m16n8k16 tile (row-major A, column-major B, fp32 accumulators)
 __device__ __forceinline__ void tc_mma(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
   asm("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
@@ -876,9 +893,11 @@ struct TcShared {
   int b_idx[TC_WARPS * 16];
   float4 s_acc[2][NTHREADS];   // {acc.x, acc.y, comp.x, comp.y} per voxel V
   // conj(r) of the thread's (voxel, element) pairs, packed over the two elements i of a
-  // (voxel, k-step): {re, re}, {im, im}, {-im, -im}
-  float2 s_cr[2 * TC_KS][3][NTHREADS];
-  float2 s_dx[4 * TC_KS][NTHREADS];   // |c_e - x| of the pairs as {left side, right side}, the other 0
+  // (voxel, k-step): {re, re, im, im}, and {-im, -im}
+  float4 s_cr[2 * TC_KS][NTHREADS];
+  float2 s_cin[2 * TC_KS][NTHREADS];
+  float s_dx[4 * TC_KS][NTHREADS];    // |c_e - x| of the pairs, negative on the left side (e < emid)
+  dfl s_ux[4 * TC_KS][NTHREADS];      // u_rx of the pairs (the receive re-anchors)
 };
 
 // Extra shared memory of the derivative variant: the pairs' receive delays and the
@@ -917,7 +936,9 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
   auto& b_idx = sh.b_idx;
   auto& s_acc = sh.s_acc;
   auto& s_cr = sh.s_cr;
+  auto& s_cin = sh.s_cin;
   auto& s_dx = sh.s_dx;
+  auto& s_ux = sh.s_ux;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int g = lane >> 2, q = lane & 3;
   int4* seg_blk = d.seg + (size_t)blockIdx.x * NTHREADS * (size_t)d.seg_cap * PW_SEG_INT4;
@@ -1010,15 +1031,15 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
               const int e = min(e0 + 8 * s + 2 * q + i, d.ne - 1);
               const dfl cm = d.el_m[e];
               const float dx = fabsf((cm.x - xm.x) + (cm.y - xm.y));
-              const bool left = e0 + 8 * s + 2 * q + i < emid[V];
-              s_dx[2 * TC_KS * V + 2 * s + i][tid] = make_float2(left ? dx : 0.0f, left ? 0.0f : dx);
+              s_dx[2 * TC_KS * V + 2 * s + i][tid] = (e0 + 8 * s + 2 * q + i < emid[V]) ? -dx : dx;
               const dfl urx = df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2));
+              s_ux[2 * TC_KS * V + 2 * s + i][tid] = urx;
               const float2 r = cis_ku(1, urx);
               if constexpr (DERIV) dsh->s_urx[2 * TC_KS * V + 2 * s + i][tid] = urx.x + urx.y;
-              float* c = reinterpret_cast<float*>(&s_cr[TC_KS * V + s][0][tid]);
+              float* c = reinterpret_cast<float*>(&s_cr[TC_KS * V + s][tid]);
               c[i] = r.x;
-              reinterpret_cast<float*>(&s_cr[TC_KS * V + s][1][tid])[i] = -r.y;
-              reinterpret_cast<float*>(&s_cr[TC_KS * V + s][2][tid])[i] = r.y;
+              c[2 + i] = -r.y;
+              reinterpret_cast<float*>(&s_cin[TC_KS * V + s][tid])[i] = r.y;
             }
         }
         float H[3][4];
@@ -1056,13 +1077,11 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
           // receive phasors re-anchored exactly at the chunk's first bin
 #pragma unroll
           for (int V = 0; V < 2; ++V) {
-            const dfl xu = d.col_u[vic[V]], zu2 = d.row_u2[vjc[V]];
 #pragma unroll
             for (int s = 0; s < TC_KS; ++s)
 #pragma unroll
               for (int i = 0; i < 2; ++i) {
-                const int e = min(e0 + 8 * s + 2 * q + i, d.ne - 1);
-                const float2 c = cis_ku(kc_hi, df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], xu)), zu2)));
+                const float2 c = cis_ku(kc_hi, s_ux[2 * TC_KS * V + 2 * s + i][tid]);
                 if (i == 0) {
                   pr[V][s].x = c.x;
                   pim[V][s].x = c.y;
@@ -1106,8 +1125,8 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
                   for (int s = 0; s < TC_KS; ++s)
 #pragma unroll
                     for (int i = 0; i < 2; ++i) {
-                      const float2 dlr = s_dx[2 * TC_KS * V + 2 * s + i][tid];
-                      const float u = fmaf(dlr.x, en[V].y, dlr.y * en[V].z);
+                      const float sd = s_dx[2 * TC_KS * V + 2 * s + i][tid];
+                      const float u = fabsf(sd) * (sd < 0.0f ? en[V].y : en[V].z);
                       bw[V][s][i] = (u < 1.0f) ? win_t<WIN>(d.window_par, inv_par, u) * en[V].w : 0.0f;
                     }
                 }
@@ -1147,16 +1166,17 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
                   const float2 Pr = pr[V][s], Pi = pim[V][s];
                   rre[V] = __fmul2_rn(bb, Pr);
                   rim[V] = __fmul2_rn(bb, Pi);
-                  const float2 cre = s_cr[TC_KS * V + s][0][tid], cim = s_cr[TC_KS * V + s][1][tid],
-                               cimn = s_cr[TC_KS * V + s][2][tid];
+                  const float4 c4 = s_cr[TC_KS * V + s][tid];
+                  const float2 cre = make_float2(c4.x, c4.y), cim = make_float2(c4.z, c4.w),
+                               cimn = s_cin[TC_KS * V + s][tid];
                   pr[V][s] = __ffma2_rn(Pi, cimn, __fmul2_rn(Pr, cre));
                   pim[V][s] = __ffma2_rn(Pi, cre, __fmul2_rn(Pr, cim));
                 }
                 unsigned ah[4], al[4];
-                tc_split(rre[0].x, rre[0].y, ah[0], al[0]);
-                tc_split(rre[1].x, rre[1].y, ah[1], al[1]);
-                tc_split(rim[0].x, rim[0].y, ah[2], al[2]);
-                tc_split(rim[1].x, rim[1].y, ah[3], al[3]);
+                tc_split_mx(rre[0].x, rre[0].y, ah[0], al[0]);
+                tc_split_mx(rre[1].x, rre[1].y, ah[1], al[1]);
+                tc_split_mx(rim[0].x, rim[0].y, ah[2], al[2]);
+                tc_split_mx(rim[1].x, rim[1].y, ah[3], al[3]);
                 // product-major order: consecutive mma.sync update different accumulators
 #pragma unroll
                 for (int j = 0; j < 3; ++j) tc_mma(H[j], ah, bf[j].x, bf[j].y);
@@ -1172,8 +1192,8 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
                     const float2 uu = make_float2(dsh->s_urx[2 * TC_KS * V + 2 * s][tid],
                                                   dsh->s_urx[2 * TC_KS * V + 2 * s + 1][tid]);
                     const float2 r2 = __fmul2_rn(rre[V], uu), i2 = __fmul2_rn(rim[V], uu);
-                    tc_split(r2.x, r2.y, ah2[V], al2[V]);
-                    tc_split(i2.x, i2.y, ah2[2 + V], al2[2 + V]);
+                    tc_split_mx(r2.x, r2.y, ah2[V], al2[V]);
+                    tc_split_mx(i2.x, i2.y, ah2[2 + V], al2[2 + V]);
                   }
 #pragma unroll
                   for (int j = 0; j < 3; ++j) tc_mma(HP[j], ah2, bf[j].x, bf[j].y);
@@ -1367,10 +1387,10 @@ __global__ void __launch_bounds__(NTHREADS, 3)
 pw_tc_deriv_kernel(const PWDev d, float2* __restrict__ image, float2* __restrict__ dimage, int n_tiles_x,
                    int n_tiles_z) {
   __shared__ TcShared sh;
-  __shared__ TcDerivShared dsh;
   __shared__ int s_tile;
-  extern __shared__ __align__(16) unsigned char dyn[];  // lb[ne], ub[ne] (dfl), ktop[ne]
-  dfl* lb_s = (dfl*)dyn;
+  extern __shared__ __align__(16) unsigned char dyn[];  // TcDerivShared, lb[ne], ub[ne] (dfl), ktop[ne]
+  TcDerivShared& dsh = *reinterpret_cast<TcDerivShared*>(dyn);
+  dfl* lb_s = (dfl*)(dyn + sizeof(TcDerivShared));
   dfl* ub_s = lb_s + d.ne;
   int* ktop = (int*)(ub_s + d.ne);
   const int tid = threadIdx.x;
@@ -1468,9 +1488,40 @@ static int pw_tiles_x(const PWDev& d) {
   return (d.nx + tw - 1) / tw;
 }
 
+// The tensor-core tile kernels' static shared memory and their element tables (20
+// bytes per element, dynamic) exceed the 48 KB a block may use without opting in:
+// each of them is allowed the device's maximum once per device.
+static cudaError_t pw_tc_smem_optin() {
+  static std::mutex mu;
+  static bool done[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  if (dev < 64 && done[dev]) return cudaSuccess;
+  int optin = 0;
+  if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
+  const void* fns[] = {(const void*)pw_tc_kernel<0>,       (const void*)pw_tc_kernel<1>,
+                       (const void*)pw_tc_kernel<2>,       (const void*)pw_tc_kernel<4>,
+                       (const void*)pw_tc_batch_kernel<0>, (const void*)pw_tc_batch_kernel<1>,
+                       (const void*)pw_tc_batch_kernel<2>, (const void*)pw_tc_batch_kernel<4>,
+                       (const void*)pw_tc_deriv_kernel<0>, (const void*)pw_tc_deriv_kernel<1>,
+                       (const void*)pw_tc_deriv_kernel<2>, (const void*)pw_tc_deriv_kernel<4>};
+  for (const void* f : fns) {
+    cudaFuncAttributes a;
+    if ((e = cudaFuncGetAttributes(&a, f)) != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  optin - (int)a.sharedSizeBytes)) != cudaSuccess)
+      return e;
+  }
+  if (dev < 64) done[dev] = true;
+  return cudaSuccess;
+}
+
 int pw_fused_grid(const PWDev& d, int* blocks_per_sm) {
   pw_kernel_t fn = pw_pick(d);
   int dev = 0, nsm = 0, bps = 0;
+  (void)pw_tc_smem_optin();
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, NTHREADS, (size_t)d.ne * (sizeof(int) + 2 * sizeof(dfl)));
@@ -1496,7 +1547,8 @@ cudaError_t launch_pw_fused(const PWDev& d, int grid, float2* image, float* weig
   const int ntx = pw_tiles_x(d), ntz = (d.nz + TILE_Z - 1) / TILE_Z;
   const size_t smem = (size_t)d.ne * (sizeof(int) + 2 * sizeof(dfl));
   // each launch draws tiles from a fresh counter
-  cudaError_t e = cudaMemsetAsync(d.counters + 3, 0, sizeof(unsigned long long), s);
+  cudaError_t e = pw_tc_smem_optin();
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.counters + 3, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
   if (pw_variant_of(d) == TC_VARIANT && (e = launch_pw_tc_prep(d, s)) != cudaSuccess) return e;
   pw_pick(d)<<<grid, NTHREADS, smem, s>>>(d, image, weights, ntx, ntz);
@@ -1530,7 +1582,8 @@ cudaError_t launch_pw_tc_deriv(const PWDev& d, float2* image, float2* dimage, cu
   cudaError_t e = cudaMemsetAsync(d.counters, 0, 5 * sizeof(unsigned long long), s);
   if (e == cudaSuccess) e = launch_pw_tc_prep(d, s);
   if (e != cudaSuccess) return e;
-  const size_t smem = (size_t)d.ne * (sizeof(int) + 2 * sizeof(dfl));
+  const size_t smem = sizeof(TcDerivShared) + (size_t)d.ne * (sizeof(int) + 2 * sizeof(dfl));
+  if ((e = pw_tc_smem_optin()) != cudaSuccess) return e;
   int dev = 0, nsm = 0, bps = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -1557,6 +1610,7 @@ static pw_tc_batch_t pw_tc_batch_pick(int window_id) {
 
 int pw_tc_batch_grid(int max_ne, int window_id, int* blocks_per_sm) {
   int dev = 0, nsm = 0, bps = 0;
+  (void)pw_tc_smem_optin();
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pw_tc_batch_pick(window_id), NTHREADS,
@@ -1567,7 +1621,8 @@ int pw_tc_batch_grid(int max_ne, int window_id, int* blocks_per_sm) {
 }
 
 cudaError_t launch_pw_tc_batch(const PWBatchDev& B, int window_id, int grid, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(B.counter, 0, sizeof(unsigned long long), s);
+  cudaError_t e = pw_tc_smem_optin();
+  if (e == cudaSuccess) e = cudaMemsetAsync(B.counter, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
   const size_t smem = (size_t)B.max_ne * (sizeof(int) + 2 * sizeof(dfl));
   pw_tc_batch_pick(window_id)<<<grid, NTHREADS, smem, s>>>(B);
@@ -2478,6 +2533,20 @@ __device__ __forceinline__ float2 cis_ku_fast(int k, dfl u) {
   return make_float2(cs, sn);
 }
 
+// the adjoint's receive table: u_rx in double-float and the step e^{2 pi i u_rx} of every
+// (voxel, element) pair, formed as pw_adjoint_tc_kernel forms them without the table
+__global__ void __launch_bounds__(256) pw_rx_table_kernel(const PWDev d) {
+  const size_t n = (size_t)d.nx * d.nz * d.ne;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t v = idx / d.ne;
+    const int e = (int)(idx - v * d.ne);
+    const int i = (int)(v / d.nz), j = (int)(v - (size_t)i * d.nz);
+    const dfl urx = df_sqrt(df_add(df_sqr(df_sub(d.el_u[e], d.col_u[i])), d.row_u2[j]));
+    const float2 st = cis_ku_fast(1, urx);
+    d.rx_tab[idx] = make_float4(urx.x, urx.y, st.x, st.y);
+  }
+}
+
 template <int WIN>
 __global__ void __launch_bounds__(ADJ_TC_WARPS * 32, 2)
 pw_adjoint_tc_kernel(const PWDev d, const float2* __restrict__ cot, const float* __restrict__ invw,
@@ -2486,6 +2555,7 @@ pw_adjoint_tc_kernel(const PWDev d, const float2* __restrict__ cot, const float*
   __shared__ uint4 sB[ADJ_TB][3][32];            // B fragments {b0 hi, b1 hi, b0 lo, b1 lo}
   __shared__ float2 sAp[ADJ_TB][8];              // {1/L_left, 1/L_right} per bin, voxel (1e30: no side)
   __shared__ int sVox[8][3];                     // column, row, first element right of x
+  __shared__ int2 sRng[ADJ_TB][8];               // aperture element range {ilb, iub} per bin, voxel
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int g = lane >> 2, q = lane & 3;
   const int kc_lo = d.k_lb + blockIdx.x * ADJ_TB, kc_hi = min(kc_lo + ADJ_TB, d.k_ub + 1) - 1;
@@ -2542,11 +2612,13 @@ pw_adjoint_tc_kernel(const PWDev d, const float2* __restrict__ cot, const float*
     } else if (tid >= 128 && tid < 128 + ADJ_TB * 8) {
       const int b = (tid - 128) >> 3, vv = (tid - 128) & 7;
       float il = 1.0e30f, ir = 1.0e30f;
+      int2 rng = make_int2(d.ne, -1);
       if (vv < nv && b < nb) {
         const int i = sVox[vv][0], j = sVox[vv][1];
         const dfl xm = d.col_m[i];
         int ilb, iub;
         aperture(d.col_p[i], d.row_p[j], d.g[kc_hi - b - d.k_lb], d.ne, ilb, iub);
+        rng = make_int2(ilb, iub);
         if (ilb < d.ne) {
           const dfl l = d.el_lb[ilb];
           const float L = (xm.x - l.x) + (xm.y - l.y);
@@ -2559,6 +2631,7 @@ pw_adjoint_tc_kernel(const PWDev d, const float2* __restrict__ cot, const float*
         }
       }
       sAp[b][vv] = make_float2(il, ir);
+      sRng[b][vv] = rng;
     }
     __syncthreads();
     // B fragments: lane (gg, qq) of n-tile j holds rows 2qq, 2qq+1 (voxels, Re block) and
@@ -2579,6 +2652,30 @@ pw_adjoint_tc_kernel(const PWDev d, const float2* __restrict__ cot, const float*
       sB[b][j][ln] = o;
     }
     __syncthreads();
+    // The bins in which one of the warp's 16 elements lies in the aperture range of one
+    // of the 8 voxels: elements outside [ilb, iub] have window argument u >= 1 (weight
+    // 0), so the other bins add nothing and are skipped, and with them the whole group
+    // when none is left.  Lane p checks (bin p / 8, voxel p % 8) and p + 32.
+    unsigned act = 0;
+    {
+      const int w_lo = e_pass + 16 * warp, w_hi = min(w_lo + 15, d.ne - 1);
+      bool h0 = false, h1 = false;
+      if (lane < ADJ_TB * 8) {
+        const int2 r = sRng[lane >> 3][lane & 7];
+        h0 = max(r.x, w_lo) <= min(r.y, w_hi);
+      }
+      if (lane + 32 < ADJ_TB * 8) {
+        const int2 r = sRng[(lane + 32) >> 3][lane & 7];
+        h1 = max(r.x, w_lo) <= min(r.y, w_hi);
+      }
+      const unsigned m0 = __ballot_sync(0xffffffffu, h0), m1 = __ballot_sync(0xffffffffu, h1);
+#pragma unroll
+      for (int b = 0; b < ADJ_TB; ++b) {
+        const unsigned byte = (b < 4) ? (m0 >> (8 * b)) : (m1 >> (8 * (b - 4)));
+        if (byte & 0xffu) act |= 1u << b;
+      }
+    }
+    if (act == 0) continue;
     // conj(R) of elements (eA, eB) x voxels (2q, 2q+1)
     float2 P[2][2], st[2][2];   // [element][voxel]: conj(r^k) and the step r
     float dl[2][2], dr[2][2];   // distances to the voxel by aperture side
@@ -2586,16 +2683,24 @@ pw_adjoint_tc_kernel(const PWDev d, const float2* __restrict__ cot, const float*
     for (int t2 = 0; t2 < 2; ++t2) {
       const int vv = 2 * q + t2;
       const int i = sVox[vv][0], j = sVox[vv][1];
-      const dfl xm = d.col_m[i], xu = d.col_u[i], zu2 = d.row_u2[j];
+      const dfl xm = d.col_m[i];
       const int emid = sVox[vv][2];
 #pragma unroll
       for (int m = 0; m < 2; ++m) {
-        const dfl cm = m ? cmB : cmA, cu = m ? cuB : cuA;
+        const dfl cm = m ? cmB : cmA;
         const int e = m ? eB : eA;
-        const dfl urx = df_sqrt(df_add(df_sqr(df_sub(cu, xu)), zu2));
+        dfl urx;
+        if (d.rx_tab) {
+          const float4 rx = d.rx_tab[(size_t)(v0 + min(vv, nv - 1)) * d.ne + min(e, d.ne - 1)];
+          urx = make_float2(rx.x, rx.y);
+          st[m][t2] = make_float2(rx.z, rx.w);
+        } else {
+          const dfl cu = m ? cuB : cuA;
+          urx = df_sqrt(df_add(df_sqr(df_sub(cu, d.col_u[i])), d.row_u2[j]));
+          st[m][t2] = cis_ku_fast(1, urx);
+        }
         const float2 c = cis_ku_fast(kc_hi, urx);
         P[m][t2] = make_float2(c.x, -c.y);
-        st[m][t2] = cis_ku_fast(1, urx);
         const float dx = fabsf((cm.x - xm.x) + (cm.y - xm.y));
         const bool ok = (vv < nv) && (e < d.ne);
         const bool left = e < emid;
@@ -2605,7 +2710,12 @@ pw_adjoint_tc_kernel(const PWDev d, const float2* __restrict__ cot, const float*
     }
 #pragma unroll
     for (int b = 0; b < ADJ_TB; ++b) {
-      if (b < nb) {
+      if (b < nb && !((act >> b) & 1u)) {
+#pragma unroll
+        for (int t2 = 0; t2 < 2; ++t2)
+#pragma unroll
+          for (int m = 0; m < 2; ++m) P[m][t2] = cmul(P[m][t2], st[m][t2]);
+      } else if (b < nb) {
         float rr[2][2], ri[2][2];
 #pragma unroll
         for (int t2 = 0; t2 < 2; ++t2) {
@@ -2667,6 +2777,7 @@ cudaError_t launch_pw_adjoint(const PWDev& d, const float2* cot, const float* in
   if (e == cudaSuccess) e = cudaMemsetAsync(gmax, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
   absmax_f32_kernel<<<608, 256, 0, s>>>(reinterpret_cast<const float*>(cot), 2 * (size_t)nvox, gmax);
+  if (d.rx_tab) pw_rx_table_kernel<<<1216, 256, 0, s>>>(d);
   const dim3 grid((d.K + ADJ_TB - 1) / ADJ_TB, (unsigned)((nvox + ADJ_TC_SLICE - 1) / ADJ_TC_SLICE),
                   (d.ne + ADJ_TC_WARPS * 16 - 1) / (ADJ_TC_WARPS * 16));
   const int nt = ADJ_TC_WARPS * 32;
