@@ -922,7 +922,11 @@ struct TcDerivShared {
 // a second Horner chain beside each first one: going down the bins, Q <- (Q + P) t
 // before P <- P t + Y, and a chunk ending at bin kc_lo contributes t^kc_lo (kc_lo P + Q).
 // dimage receives Draw (scaled like the image).
-template <int WIN, bool DERIV>
+//
+// BATCH (the persistent batch kernel, whose descriptor lies in global memory) reads the
+// descriptor fields of the bin loop once per tile; the per-frame kernels read their
+// parameters' fields where they are used (constant-bank operands, no registers held).
+template <int WIN, bool DERIV, bool BATCH = false>
 __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles_x, int n_tiles_z, TcShared& sh,
                                            const dfl* lb_s, const dfl* ub_s, int* ktop, float2* __restrict__ image,
                                            float* __restrict__ weights, unsigned long long& n_active,
@@ -944,6 +948,9 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
   int4* seg_blk = d.seg + (size_t)blockIdx.x * NTHREADS * (size_t)d.seg_cap * PW_SEG_INT4;
   const float inv_par = (d.window_par > 0.0f) ? 1.0f / d.window_par : 0.0f;
   const float inv_sigma = 1.0f / tc_scale(*d.tc_max);
+  const int b_k_lb = d.k_lb, b_ne = d.ne, b_tc_S = d.tc_S;
+  const float b_window_par = d.window_par;
+#define TC_D(field) (BATCH ? b_##field : d.field)
   const int tb = (d.tc_tb > 0 && d.tc_tb < TC_TB) ? d.tc_tb : TC_TB;   // bins per flush (a launch shape)
   {
     int tx, tz;
@@ -987,7 +994,7 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
       // or a half-width that is not positive) gets 1/L = 1e30, which sends its elements
       // to u >= 1 and keeps the other side's (distance 0 on this side) at u = d / L.
       float il = 1.0e30f, ir = 1.0e30f;
-      if (ilb < d.ne) {
+      if (ilb < TC_D(ne)) {
         const dfl l = lb_s[ilb];
         const float L = (bxm.x - l.x) + (bxm.y - l.y);
         if (L > 0.0f) il = __fdividef(1.0f, L);
@@ -1015,7 +1022,7 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
       for (int e0 = E_lo; e0 <= E_hi; e0 += TC_EP) {
         int kt = -1;
         for (int e = max(e0, 0); e < min(e0 + TC_EP, E_hi + 1); ++e) kt = max(kt, ktop[e]);
-        if (kt < d.k_lb) continue;
+        if (kt < TC_D(k_lb)) continue;
         if (tid == 0)
           n_exec += (unsigned long long)(kt - d.k_lb + 1) * TC_EP * min(TC_NA, d.na - a0) * (TC_WARPS * 16);
         // the thread's (voxel, element) pairs: V, element e0 + 8s + 2q + i
@@ -1072,8 +1079,8 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
         // the pairs' weights of the segment in effect, recomputed when a voxel enters a new segment
         float bw[2][TC_KS][2];
         int wid[2] = {-1, -1};
-        for (int kc_hi = kt; kc_hi >= d.k_lb; kc_hi -= tb) {
-          const int kc_lo = max(d.k_lb, kc_hi - (tb - 1));
+        for (int kc_hi = kt; kc_hi >= TC_D(k_lb); kc_hi -= tb) {
+          const int kc_lo = max(TC_D(k_lb), kc_hi - (tb - 1));
           // receive phasors re-anchored exactly at the chunk's first bin
 #pragma unroll
           for (int V = 0; V < 2; ++V) {
@@ -1127,7 +1134,7 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
                     for (int i = 0; i < 2; ++i) {
                       const float sd = s_dx[2 * TC_KS * V + 2 * s + i][tid];
                       const float u = fabsf(sd) * (sd < 0.0f ? en[V].y : en[V].z);
-                      bw[V][s][i] = (u < 1.0f) ? win_t<WIN>(d.window_par, inv_par, u) * en[V].w : 0.0f;
+                      bw[V][s][i] = (u < 1.0f) ? win_t<WIN>(TC_D(window_par), inv_par, u) * en[V].w : 0.0f;
                     }
                 }
               }
@@ -1152,7 +1159,7 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
                   H[j][2 * V] = fmaf(hr, t.x, -hi * t.y);
                   H[j][2 * V + 1] = fmaf(hr, t.y, hi * t.x);
                 }
-              const uint4* Bk = Bpe + (size_t)(k - d.k_lb) * d.tc_S * 96;
+              const uint4* Bk = Bpe + (size_t)(k - TC_D(k_lb)) * TC_D(tc_S) * 96;
 #pragma unroll
               for (int s = 0; s < TC_KS; ++s) {
                 uint4 bf[3];
@@ -1282,6 +1289,7 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
     __syncthreads();
   }
 }
+#undef TC_D
 
 // the per-frame statistics of pw_tc_tile, added to the frame's counters
 __device__ __forceinline__ void pw_tc_flush_counts(const PWDev& d, unsigned long long& n_active,
@@ -1375,7 +1383,7 @@ __global__ void __launch_bounds__(NTHREADS, 4) pw_tc_batch_kernel(const PWBatchD
     }
     __syncthreads();
     const int ntx = (d.nx + TC_TILE_X - 1) / TC_TILE_X, ntz = (d.nz + TILE_Z - 1) / TILE_Z;
-    pw_tc_tile<WIN, false>(d, s_tile, ntx, ntz, sh, lb_s, ub_s, ktop, B.images[f], B.weights[f], n_active, n_empty,
+    pw_tc_tile<WIN, false, true>(d, s_tile, ntx, ntz, sh, lb_s, ub_s, ktop, B.images[f], B.weights[f], n_active, n_empty,
                            n_exec);
   }
   if (cur >= 0) pw_tc_flush_counts(B.frames[cur], n_active, n_empty, n_exec);
