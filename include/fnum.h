@@ -346,7 +346,10 @@ int fnum_pw_plan_set_sound_speed(fnum_plan* plan, double c_0);
    of the band spectra (device float2 [n_elements][n_bins][n_angles]; a change
    dX of the spectra changes L by 2 Re sum conj(dL/dX*) dX).  The first call
    allocates the plan's gradient buffers (a 1/W table of n_x n_z n_bins floats
-   among them).  Synchronises `stream`. */
+   among them) and, if the memory is there, a receive table of 16 bytes per
+   voxel and element (n_x n_z n_elements; 537 MB at 512 x 512 x 128) that
+   speeds up dL/dX* -- without it the kernel forms the same values itself.
+   Synchronises `stream`. */
 int fnum_pw_sharpness_grad(fnum_plan* plan, const void* d_rf, int rf_is_double, double* loss, double* dloss_dc,
                            void* d_grad_spectra, void* stream);
 
