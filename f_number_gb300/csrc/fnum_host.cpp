@@ -747,9 +747,14 @@ int make_pw_plan(const fnum_pw_desc* d, const double* angles, int na, int flags,
     D.seg = seg;
     P->info.scratch_bytes =
         (long long)P->max_grid * fnum::NTHREADS * D.seg_cap * fnum::PW_SEG_INT4 * (long long)sizeof(int4);
-    // tensor-core variant: spectra as mma fragments (96 uint4 per bin and group of 8 elements)
+    // tensor-core variant: spectra as mma fragments (32 uint4 per n-tile, bin and group of 8 elements)
     D.tc_S = (ne + 7) / 8 + fnum::TC_KS - 1;   // a pass may start in the last group of 8
-    const size_t n_tc = (size_t)((na + fnum::TC_NA - 1) / fnum::TC_NA) * D.K * D.tc_S * 96;
+    D.tc_nt = fnum::tc_ntiles_for(na);
+    // the fragments in the layout of the plan's passes, or of 12-angle passes (the
+    // derivative kernel's), whichever is larger
+    size_t n_tc = 0;
+    for (int nt : {3, D.tc_nt})
+      n_tc = std::max(n_tc, (size_t)((na + 4 * nt - 1) / (4 * nt)) * D.K * D.tc_S * 32 * nt);
     if ((s = P->alloc(&D.tc_B, n_tc))) goto fail;
     if ((s = P->alloc(&D.tc_max, 1))) goto fail;
     P->info.scratch_bytes += (long long)(n_tc * sizeof(uint4) + sizeof(unsigned));
@@ -1552,9 +1557,10 @@ struct fnum_batch {
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t start = nullptr;
   std::vector<cudaEvent_t> done;   // per frame, recorded when the frame's image is complete
-  // persistent tensor-core launches, one per window of the compounded tensor-core frames
+  // persistent tensor-core launches, one per window and pass width of the compounded tensor-core frames
   struct TcGroup {
     int window_id = 0, grid = 0;
+    int nt = 3;                     // n-tiles per angle pass of the group's frames
     std::vector<int> frames;        // batch frame indices, largest first
     fnum::PWBatchDev dev{};
   };
@@ -1617,7 +1623,7 @@ int build_tc_group(fnum_batch* B, fnum_batch::TcGroup& G, fnum_plan* const* plan
   dev.n_frames = (int)G.frames.size();
   dev.max_ne = max_ne;
   dev.seg_cap = seg_cap;
-  G.grid = fnum::pw_tc_batch_grid(max_ne, G.window_id, nullptr);
+  G.grid = fnum::pw_tc_batch_grid(max_ne, G.window_id, G.nt, nullptr);
   fnum::PWDev* d_frames = nullptr;
   float2** d_img = nullptr;
   float** d_w = nullptr;
@@ -1684,18 +1690,19 @@ int fnum_batch_create(fnum_plan* const* plans, int n, const void* const* d_rf, c
   for (int i = 0; i < n && e == cudaSuccess; ++i) e = cudaEventCreate(&B->done[i]);
   for (int i = 0; i < k && e == cudaSuccess; ++i) e = cudaStreamCreateWithFlags(&st[i], cudaStreamNonBlocking);
   for (int i = 0; i < k && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&fj[i], cudaEventDisableTiming);
-  // compounded tensor-core frames go to persistent launches (one per window), the others
+  // compounded tensor-core frames go to persistent launches (one per window and pass width), the others
   // keep a launch per frame on the branches
   std::vector<char> persistent(n, 0);
   for (int f : order) {
     if (!tc_persistent(plans[f])) continue;
     persistent[f] = 1;
-    const int w = plans[f]->pw.window_id;
+    const int w = plans[f]->pw.window_id, nt = plans[f]->pw.tc_nt == 4 ? 4 : 3;
     size_t gi = 0;
-    while (gi < B->groups.size() && B->groups[gi].window_id != w) ++gi;
+    while (gi < B->groups.size() && (B->groups[gi].window_id != w || B->groups[gi].nt != nt)) ++gi;
     if (gi == B->groups.size()) {
       B->groups.emplace_back();
       B->groups.back().window_id = w;
+      B->groups.back().nt = nt;
     }
     B->groups[gi].frames.push_back(f);   // `order` is largest first
     ++B->persistent_frames;
@@ -1741,7 +1748,7 @@ int fnum_batch_create(fnum_plan* const* plans, int n, const void* const* d_rf, c
     }
     for (auto& G : B->groups) {
       if (s) break;
-      e = fnum::launch_pw_tc_batch(G.dev, G.window_id, G.grid, st[0]);
+      e = fnum::launch_pw_tc_batch(G.dev, G.window_id, G.nt, G.grid, st[0]);
       for (size_t j = 0; j < G.frames.size() && e == cudaSuccess; ++j)
         e = cudaEventRecordWithFlags(B->done[G.frames[j]], st[0], cudaEventRecordExternal);
       if (e != cudaSuccess) s = cuda_status(e);

@@ -21,6 +21,10 @@ constexpr int KCHUNK = 64;
 // tensor-core plane-wave kernel: 4 warps of 16 voxels, TC_TILE_X columns x TILE_Z rows
 constexpr int TC_TILE_X = 2;
 constexpr int TC_NA = 12;   // angles per angle pass (3 mma n-tiles of 4 complex angles)
+// A plane-wave plan's tensor-core kernel runs passes of 3 n-tiles (12 angles) or, when
+// that takes fewer passes (13-16, 25-32, 37-48 angles), of 4 (16 angles): each pass
+// forms the same A operands, so fewer passes is less work.
+inline int tc_ntiles_for(int na) { return ((na + 15) / 16 < (na + TC_NA - 1) / TC_NA) ? 4 : 3; }
 constexpr int TC_EP = 16;   // elements per pass: TC_KS mma k-steps of 8 complex elements
 constexpr int TC_KS = TC_EP / 8;
 constexpr int TC_VARIANT = 9;
@@ -75,6 +79,7 @@ struct PWDev {
   uint4* tc_B;
   unsigned* tc_max;
   int tc_S;            // element groups of 8 in tc_B (TC_KS - 1 zero groups of padding included)
+  int tc_nt;           // mma n-tiles per angle pass of the tensor-core kernel (3 or 4; 0 reads as 3)
   unsigned long long* counters;   // [0] active terms, [1] zero-weight bins, [2] error bits,
                                   // [3] tile counter, [4] executed recurrence steps
   // the per-voxel FP32 kernel reads the reference's float geometry
@@ -197,12 +202,14 @@ cudaError_t launch_pw_fused(const PWDev& d, int grid, float2* image, float* weig
 // the compounded image and, in dimage, Draw with dI/dc = -(2 pi i / c) Draw (tensor cores;
 // prepares the fragments itself)
 cudaError_t launch_pw_tc_deriv(const PWDev& d, float2* image, float2* dimage, cudaStream_t s);
-// the tensor-core variant's spectra scale and B fragments for frame d (before a batch launch)
-cudaError_t launch_pw_tc_prep(const PWDev& d, cudaStream_t s);
+// the tensor-core variant's spectra scale and B fragments for frame d (before a batch launch),
+// laid out for passes of nt n-tiles (0: the plan's own, d.tc_nt)
+cudaError_t launch_pw_tc_prep(const PWDev& d, cudaStream_t s, int nt = 0);
 // tiles of a frame for the tensor-core kernel; grid of the batch kernel with all blocks resident
 int pw_tc_tiles(const PWDev& d);
-int pw_tc_batch_grid(int max_ne, int window_id, int* blocks_per_sm);
-cudaError_t launch_pw_tc_batch(const PWBatchDev& B, int window_id, int grid, cudaStream_t s);
+// nt: the n-tiles per angle pass of every frame of the launch (frames are grouped by it)
+int pw_tc_batch_grid(int max_ne, int window_id, int nt, int* blocks_per_sm);
+cudaError_t launch_pw_tc_batch(const PWBatchDev& B, int window_id, int nt, int grid, cudaStream_t s);
 cudaError_t launch_pw_plain(const PWDev& d, float2* image, float* weights, cudaStream_t s);
 constexpr int M_MAXE = 256;   // elements supported by the das_pw.m-semantics kernel
 cudaError_t launch_pw_m(const PWDev& d, int compound, float2* image, float* weights, cudaStream_t s);

@@ -844,26 +844,27 @@ __global__ void __launch_bounds__(256) tc_absmax_kernel(const PWDev d, unsigned*
 }
 
 
-// B fragments of the spectra: for angle pass ap, bin kk, element group s (elements
-// 8s .. 8s+7), n-tile j (angles ap*TC_NA + 4j .. +3) and lane (g = lane/4, q = lane%4):
+// B fragments of the spectra: for angle pass ap (nt n-tiles of 4 angles), bin kk, element
+// group s (elements 8s .. 8s+7), n-tile j (angles ap*4nt + 4j .. +3) and lane (g = lane/4,
+// q = lane%4):
 //   b0 = {B[2q][g], B[2q+1][g]}, b1 = {B[2q+8][g], B[2q+9][g]} as fp16 hi, then lo,
 // with rows 0..7 the Rr rows and 8..15 the Ri rows of the group's elements and
 // column g = 2 (angle) + (0: Gr, 1: Gi).
-__global__ void __launch_bounds__(256) tc_prep_kernel(const PWDev d, int n_ap) {
-  const size_t n = (size_t)n_ap * d.K * d.tc_S * 3 * 32;
+__global__ void __launch_bounds__(256) tc_prep_kernel(const PWDev d, int n_ap, int nt) {
+  const size_t n = (size_t)n_ap * d.K * d.tc_S * nt * 32;
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float sigma = tc_scale(*d.tc_max);
   const int lane = (int)(i & 31);
   size_t r = i >> 5;
-  const int j = (int)(r % 3);
-  r /= 3;
+  const int j = (int)(r % nt);
+  r /= nt;
   const int s = (int)(r % d.tc_S);
   r /= d.tc_S;
   const int kk = (int)(r % d.K);
   const int ap = (int)(r / d.K);
   const int g = lane >> 2, q = lane & 3;
-  const int a = ap * TC_NA + 4 * j + (g >> 1), part = g & 1;
+  const int a = ap * 4 * nt + 4 * j + (g >> 1), part = g & 1;
   float rr[2], ri[2];
 #pragma unroll
   for (int t = 0; t < 2; ++t) {
@@ -926,7 +927,7 @@ struct TcDerivShared {
 // BATCH (the persistent batch kernel, whose descriptor lies in global memory) reads the
 // descriptor fields of the bin loop once per tile; the per-frame kernels read their
 // parameters' fields where they are used (constant-bank operands, no registers held).
-template <int WIN, bool DERIV, bool BATCH = false>
+template <int WIN, bool DERIV, bool BATCH = false, int NT = 3>
 __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles_x, int n_tiles_z, TcShared& sh,
                                            const dfl* lb_s, const dfl* ub_s, int* ktop, float2* __restrict__ image,
                                            float* __restrict__ weights, unsigned long long& n_active,
@@ -952,6 +953,8 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
   const float b_window_par = d.window_par;
 #define TC_D(field) (BATCH ? b_##field : d.field)
   const int tb = (d.tc_tb > 0 && d.tc_tb < TC_TB) ? d.tc_tb : TC_TB;   // bins per flush (a launch shape)
+  constexpr int NA_P = 4 * NT;     // angles per pass
+  constexpr int NB = 32 * NT;      // uint4 of B fragments per element group and bin
   {
     int tx, tz;
     tile_coords(tile, n_tiles_x, n_tiles_z, tx, tz);
@@ -1009,22 +1012,22 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
     s_acc[0][tid] = s_acc[1][tid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if constexpr (DERIV) dsh->s_dacc[0][tid] = dsh->s_dacc[1][tid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 
-    for (int a0 = 0; a0 < d.na; a0 += TC_NA) {
-      float2 tph[2][3];   // transmit phasor of (voxel V, angle a0 + 4j + q)
+    for (int a0 = 0; a0 < d.na; a0 += NA_P) {
+      float2 tph[2][NT];   // transmit phasor of (voxel V, angle a0 + 4j + q)
 #pragma unroll
       for (int V = 0; V < 2; ++V)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) {
+        for (int j = 0; j < NT; ++j) {
           const int aa = min(a0 + 4 * j + q, d.na - 1);
           tph[V][j] = cis_ku(1, df_add(d.tx_ax[(size_t)aa * d.nx + vic[V]], d.tx_az[(size_t)aa * d.nz + vjc[V]]));
         }
-      const uint4* Bp = d.tc_B + (size_t)(a0 / TC_NA) * d.K * d.tc_S * 96;
+      const uint4* Bp = d.tc_B + (size_t)(a0 / NA_P) * d.K * d.tc_S * NB;
       for (int e0 = E_lo; e0 <= E_hi; e0 += TC_EP) {
         int kt = -1;
         for (int e = max(e0, 0); e < min(e0 + TC_EP, E_hi + 1); ++e) kt = max(kt, ktop[e]);
         if (kt < TC_D(k_lb)) continue;
         if (tid == 0)
-          n_exec += (unsigned long long)(kt - d.k_lb + 1) * TC_EP * min(TC_NA, d.na - a0) * (TC_WARPS * 16);
+          n_exec += (unsigned long long)(kt - d.k_lb + 1) * TC_EP * min(NA_P, d.na - a0) * (TC_WARPS * 16);
         // the thread's (voxel, element) pairs: V, element e0 + 8s + 2q + i
         // receive phasors r^k packed over the two elements of a (voxel, k-step): {re, re}, {im, im}
         float2 pr[2][TC_KS], pim[2][TC_KS];
@@ -1049,14 +1052,14 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
               reinterpret_cast<float*>(&s_cin[TC_KS * V + s][tid])[i] = r.y;
             }
         }
-        float H[3][4];
+        float H[NT][4];
 #pragma unroll
-        for (int j = 0; j < 3; ++j) H[j][0] = H[j][1] = H[j][2] = H[j][3] = 0.0f;
+        for (int j = 0; j < NT; ++j) H[j][0] = H[j][1] = H[j][2] = H[j][3] = 0.0f;
         // derivative chains: HQ (second chain of H), HP (the u_rx-scaled product), HPQ
-        float HQ[3][4], HP[3][4], HPQ[3][4];
+        float HQ[NT][4], HP[NT][4], HPQ[NT][4];
         if constexpr (DERIV) {
 #pragma unroll
-          for (int j = 0; j < 3; ++j)
+          for (int j = 0; j < NT; ++j)
 #pragma unroll
             for (int c = 0; c < 4; ++c) HQ[j][c] = HP[j][c] = HPQ[j][c] = 0.0f;
         }
@@ -1075,7 +1078,7 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
           b_next[bv] = bnext;
           b_idx[bv] = bs;
         }
-        const uint4* Bpe = Bp + (size_t)(e0 >> 3) * 96 + lane;
+        const uint4* Bpe = Bp + (size_t)(e0 >> 3) * NB + lane;
         // the pairs' weights of the segment in effect, recomputed when a voxel enters a new segment
         float bw[2][TC_KS][2];
         int wid[2] = {-1, -1};
@@ -1140,7 +1143,7 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
               }
               // H <- H t (derivative chains: Q <- (Q + P) t, P <- P t)
 #pragma unroll
-              for (int j = 0; j < 3; ++j)
+              for (int j = 0; j < NT; ++j)
 #pragma unroll
                 for (int V = 0; V < 2; ++V) {
                   const float hr = H[j][2 * V], hi = H[j][2 * V + 1];
@@ -1159,12 +1162,12 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
                   H[j][2 * V] = fmaf(hr, t.x, -hi * t.y);
                   H[j][2 * V + 1] = fmaf(hr, t.y, hi * t.x);
                 }
-              const uint4* Bk = Bpe + (size_t)(k - TC_D(k_lb)) * TC_D(tc_S) * 96;
+              const uint4* Bk = Bpe + (size_t)(k - TC_D(k_lb)) * TC_D(tc_S) * NB;
 #pragma unroll
               for (int s = 0; s < TC_KS; ++s) {
-                uint4 bf[3];
+                uint4 bf[NT];
 #pragma unroll
-                for (int j = 0; j < 3; ++j) bf[j] = __ldg(Bk + s * 96 + j * 32);
+                for (int j = 0; j < NT; ++j) bf[j] = __ldg(Bk + s * NB + j * 32);
                 float2 rre[2], rim[2];
 #pragma unroll
                 for (int V = 0; V < 2; ++V) {
@@ -1186,11 +1189,11 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
                 tc_split_mx(rim[1].x, rim[1].y, ah[3], al[3]);
                 // product-major order: consecutive mma.sync update different accumulators
 #pragma unroll
-                for (int j = 0; j < 3; ++j) tc_mma(H[j], ah, bf[j].x, bf[j].y);
+                for (int j = 0; j < NT; ++j) tc_mma(H[j], ah, bf[j].x, bf[j].y);
 #pragma unroll
-                for (int j = 0; j < 3; ++j) tc_mma(H[j], ah, bf[j].z, bf[j].w);
+                for (int j = 0; j < NT; ++j) tc_mma(H[j], ah, bf[j].z, bf[j].w);
 #pragma unroll
-                for (int j = 0; j < 3; ++j) tc_mma(H[j], al, bf[j].x, bf[j].y);
+                for (int j = 0; j < NT; ++j) tc_mma(H[j], al, bf[j].x, bf[j].y);
                 if constexpr (DERIV) {
                   // the second product: A scaled by the pairs' receive delays
                   unsigned ah2[4], al2[4];
@@ -1203,11 +1206,11 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
                     tc_split_mx(i2.x, i2.y, ah2[2 + V], al2[2 + V]);
                   }
 #pragma unroll
-                  for (int j = 0; j < 3; ++j) tc_mma(HP[j], ah2, bf[j].x, bf[j].y);
+                  for (int j = 0; j < NT; ++j) tc_mma(HP[j], ah2, bf[j].x, bf[j].y);
 #pragma unroll
-                  for (int j = 0; j < 3; ++j) tc_mma(HP[j], ah2, bf[j].z, bf[j].w);
+                  for (int j = 0; j < NT; ++j) tc_mma(HP[j], ah2, bf[j].z, bf[j].w);
 #pragma unroll
-                  for (int j = 0; j < 3; ++j) tc_mma(HP[j], al2, bf[j].x, bf[j].y);
+                  for (int j = 0; j < NT; ++j) tc_mma(HP[j], al2, bf[j].x, bf[j].y);
                 }
               }
             }
@@ -1217,7 +1220,7 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
           for (int V = 0; V < 2; ++V) {
             float2 part = make_float2(0.0f, 0.0f), dpart = make_float2(0.0f, 0.0f);
 #pragma unroll
-            for (int j = 0; j < 3; ++j) {
+            for (int j = 0; j < NT; ++j) {
               const int a = a0 + 4 * j + q;
               if (a < d.na) {
                 const dfl ut = df_add(d.tx_ax[(size_t)a * d.nx + vic[V]], d.tx_az[(size_t)a * d.nz + vjc[V]]);
@@ -1300,7 +1303,7 @@ __device__ __forceinline__ void pw_tc_flush_counts(const PWDev& d, unsigned long
   n_active = n_empty = n_exec = 0;
 }
 
-template <int WIN>
+template <int WIN, int NT>
 __global__ void __launch_bounds__(NTHREADS, 4)
 pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weights, int n_tiles_x, int n_tiles_z) {
   __shared__ TcShared sh;
@@ -1326,8 +1329,8 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
     __syncthreads();
     const int tile = s_tile;
     if (tile >= n_tiles) break;
-    pw_tc_tile<WIN, false>(d, tile, n_tiles_x, n_tiles_z, sh, lb_s, ub_s, ktop, image, weights, n_active, n_empty,
-                           n_exec);
+    pw_tc_tile<WIN, false, false, NT>(d, tile, n_tiles_x, n_tiles_z, sh, lb_s, ub_s, ktop, image, weights, n_active,
+                                      n_empty, n_exec);
   }
   pw_tc_flush_counts(d, n_active, n_empty, n_exec);
 }
@@ -1337,7 +1340,7 @@ pw_tc_kernel(const PWDev d, float2* __restrict__ image, float* __restrict__ weig
 // frames largest first), finds the tile's frame, and runs pw_tc_tile on it.  The frames'
 // descriptors stay in device memory (read through the cache; the host has set their
 // segment scratch to the batch's), which measured faster than a copy in shared memory.
-template <int WIN>
+template <int WIN, int NT>
 __global__ void __launch_bounds__(NTHREADS, 4) pw_tc_batch_kernel(const PWBatchDev B) {
   __shared__ TcShared sh;
   __shared__ int s_tile, s_frame;
@@ -1383,7 +1386,7 @@ __global__ void __launch_bounds__(NTHREADS, 4) pw_tc_batch_kernel(const PWBatchD
     }
     __syncthreads();
     const int ntx = (d.nx + TC_TILE_X - 1) / TC_TILE_X, ntz = (d.nz + TILE_Z - 1) / TILE_Z;
-    pw_tc_tile<WIN, false, true>(d, s_tile, ntx, ntz, sh, lb_s, ub_s, ktop, B.images[f], B.weights[f], n_active, n_empty,
+    pw_tc_tile<WIN, false, true, NT>(d, s_tile, ntx, ntz, sh, lb_s, ub_s, ktop, B.images[f], B.weights[f], n_active, n_empty,
                            n_exec);
   }
   if (cur >= 0) pw_tc_flush_counts(B.frames[cur], n_active, n_empty, n_exec);
@@ -1455,17 +1458,21 @@ static pw_kernel_t pw_pick_event_win(int window_id) {
 //      the plan's fragment scratch (PWDev::tc_B)
 // Angles beyond NA run as further passes inside the launch.  PWDev::variant
 // 0 picks by the angle count; a plan's autotuner may set another.
-static pw_kernel_t pw_pick_tc_win(int window_id) {
+static pw_kernel_t pw_pick_tc_win(int window_id, int nt) {
+  const bool n4 = nt == 4;
   switch (window_id) {
-    case 0: return pw_tc_kernel<0>;
-    case 1: return pw_tc_kernel<1>;
-    case 2: return pw_tc_kernel<2>;
-    default: return pw_tc_kernel<4>;
+    case 0: return n4 ? pw_tc_kernel<0, 4> : pw_tc_kernel<0, 3>;
+    case 1: return n4 ? pw_tc_kernel<1, 4> : pw_tc_kernel<1, 3>;
+    case 2: return n4 ? pw_tc_kernel<2, 4> : pw_tc_kernel<2, 3>;
+    default: return n4 ? pw_tc_kernel<4, 4> : pw_tc_kernel<4, 3>;
   }
 }
-static pw_kernel_t pw_variant_kernel(int v, int window_id) {
+// n-tiles per angle pass of frame d's tensor-core kernel (tc_ntiles_for, set at plan creation)
+static int pw_tc_nt(const PWDev& d) { return d.tc_nt == 4 ? 4 : 3; }
+static pw_kernel_t pw_variant_kernel(int v, const PWDev& d) {
+  const int window_id = d.window_id;
   switch (v) {
-    case TC_VARIANT: return pw_pick_tc_win(window_id);
+    case TC_VARIANT: return pw_pick_tc_win(window_id, pw_tc_nt(d));
     case 1: return pw_pick_event_win<1, 11>(window_id);
     case 2: return pw_pick_event_win<2, 4>(window_id);
     case 3: return pw_pick_event_win<2, 2>(window_id);
@@ -1486,7 +1493,7 @@ static int pw_default_variant(const PWDev& d) {
   return 4;
 }
 static pw_kernel_t pw_pick(const PWDev& d) {
-  return pw_variant_kernel(d.variant > 0 ? d.variant : pw_default_variant(d), d.window_id);
+  return pw_variant_kernel(d.variant > 0 ? d.variant : pw_default_variant(d), d);
 }
 int pw_variant_count() { return 9; }
 int pw_variant_of(const PWDev& d) { return d.variant > 0 ? d.variant : pw_default_variant(d); }
@@ -1509,12 +1516,17 @@ static cudaError_t pw_tc_smem_optin() {
   if (dev < 64 && done[dev]) return cudaSuccess;
   int optin = 0;
   if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
-  const void* fns[] = {(const void*)pw_tc_kernel<0>,       (const void*)pw_tc_kernel<1>,
-                       (const void*)pw_tc_kernel<2>,       (const void*)pw_tc_kernel<4>,
-                       (const void*)pw_tc_batch_kernel<0>, (const void*)pw_tc_batch_kernel<1>,
-                       (const void*)pw_tc_batch_kernel<2>, (const void*)pw_tc_batch_kernel<4>,
-                       (const void*)pw_tc_deriv_kernel<0>, (const void*)pw_tc_deriv_kernel<1>,
-                       (const void*)pw_tc_deriv_kernel<2>, (const void*)pw_tc_deriv_kernel<4>};
+  const void* fns[] = {
+      (const void*)pw_tc_kernel<0, 3>,       (const void*)pw_tc_kernel<1, 3>,
+      (const void*)pw_tc_kernel<2, 3>,       (const void*)pw_tc_kernel<4, 3>,
+      (const void*)pw_tc_kernel<0, 4>,       (const void*)pw_tc_kernel<1, 4>,
+      (const void*)pw_tc_kernel<2, 4>,       (const void*)pw_tc_kernel<4, 4>,
+      (const void*)pw_tc_batch_kernel<0, 3>, (const void*)pw_tc_batch_kernel<1, 3>,
+      (const void*)pw_tc_batch_kernel<2, 3>, (const void*)pw_tc_batch_kernel<4, 3>,
+      (const void*)pw_tc_batch_kernel<0, 4>, (const void*)pw_tc_batch_kernel<1, 4>,
+      (const void*)pw_tc_batch_kernel<2, 4>, (const void*)pw_tc_batch_kernel<4, 4>,
+      (const void*)pw_tc_deriv_kernel<0>,    (const void*)pw_tc_deriv_kernel<1>,
+      (const void*)pw_tc_deriv_kernel<2>,    (const void*)pw_tc_deriv_kernel<4>};
   for (const void* f : fns) {
     cudaFuncAttributes a;
     if ((e = cudaFuncGetAttributes(&a, f)) != cudaSuccess) return e;
@@ -1563,15 +1575,16 @@ cudaError_t launch_pw_fused(const PWDev& d, int grid, float2* image, float* weig
   return cudaGetLastError();
 }
 
-cudaError_t launch_pw_tc_prep(const PWDev& d, cudaStream_t s) {
+cudaError_t launch_pw_tc_prep(const PWDev& d, cudaStream_t s, int nt) {
   if (!d.tc_B || !d.tc_max) return cudaErrorInvalidValue;
+  if (nt != 3 && nt != 4) nt = pw_tc_nt(d);
   // spectra -> fp16 B fragments, scaled by a power of two set by their largest component
   cudaError_t e = cudaMemsetAsync(d.tc_max, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
   tc_absmax_kernel<<<304, 256, 0, s>>>(d, d.tc_max);
-  const int n_ap = (d.na + TC_NA - 1) / TC_NA;
-  const size_t n = (size_t)n_ap * d.K * d.tc_S * 96;
-  tc_prep_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, n_ap);
+  const int n_ap = (d.na + 4 * nt - 1) / (4 * nt);
+  const size_t n = (size_t)n_ap * d.K * d.tc_S * nt * 32;
+  tc_prep_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, n_ap, nt);
   return cudaGetLastError();
 }
 
@@ -1588,7 +1601,7 @@ static pw_tc_deriv_t pw_tc_deriv_pick(int window_id) {
 cudaError_t launch_pw_tc_deriv(const PWDev& d, float2* image, float2* dimage, cudaStream_t s) {
   if (!d.tc_B || !d.tc_max) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(d.counters, 0, 5 * sizeof(unsigned long long), s);
-  if (e == cudaSuccess) e = launch_pw_tc_prep(d, s);
+  if (e == cudaSuccess) e = launch_pw_tc_prep(d, s, 3);   // the derivative kernel runs passes of 12 angles
   if (e != cudaSuccess) return e;
   const size_t smem = sizeof(TcDerivShared) + (size_t)d.ne * (sizeof(int) + 2 * sizeof(dfl));
   if ((e = pw_tc_smem_optin()) != cudaSuccess) return e;
@@ -1607,33 +1620,34 @@ cudaError_t launch_pw_tc_deriv(const PWDev& d, float2* image, float2* dimage, cu
 int pw_tc_tiles(const PWDev& d) { return ((d.nx + TC_TILE_X - 1) / TC_TILE_X) * ((d.nz + TILE_Z - 1) / TILE_Z); }
 
 typedef void (*pw_tc_batch_t)(const PWBatchDev);
-static pw_tc_batch_t pw_tc_batch_pick(int window_id) {
+static pw_tc_batch_t pw_tc_batch_pick(int window_id, int nt) {
+  const bool n4 = nt == 4;
   switch (window_id) {
-    case 0: return pw_tc_batch_kernel<0>;
-    case 1: return pw_tc_batch_kernel<1>;
-    case 2: return pw_tc_batch_kernel<2>;
-    default: return pw_tc_batch_kernel<4>;
+    case 0: return n4 ? pw_tc_batch_kernel<0, 4> : pw_tc_batch_kernel<0, 3>;
+    case 1: return n4 ? pw_tc_batch_kernel<1, 4> : pw_tc_batch_kernel<1, 3>;
+    case 2: return n4 ? pw_tc_batch_kernel<2, 4> : pw_tc_batch_kernel<2, 3>;
+    default: return n4 ? pw_tc_batch_kernel<4, 4> : pw_tc_batch_kernel<4, 3>;
   }
 }
 
-int pw_tc_batch_grid(int max_ne, int window_id, int* blocks_per_sm) {
+int pw_tc_batch_grid(int max_ne, int window_id, int nt, int* blocks_per_sm) {
   int dev = 0, nsm = 0, bps = 0;
   (void)pw_tc_smem_optin();
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pw_tc_batch_pick(window_id), NTHREADS,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pw_tc_batch_pick(window_id, nt), NTHREADS,
                                                 (size_t)max_ne * (sizeof(int) + 2 * sizeof(dfl)));
   if (bps < 1) bps = 1;
   if (blocks_per_sm) *blocks_per_sm = bps;
   return nsm * bps;
 }
 
-cudaError_t launch_pw_tc_batch(const PWBatchDev& B, int window_id, int grid, cudaStream_t s) {
+cudaError_t launch_pw_tc_batch(const PWBatchDev& B, int window_id, int nt, int grid, cudaStream_t s) {
   cudaError_t e = pw_tc_smem_optin();
   if (e == cudaSuccess) e = cudaMemsetAsync(B.counter, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
   const size_t smem = (size_t)B.max_ne * (sizeof(int) + 2 * sizeof(dfl));
-  pw_tc_batch_pick(window_id)<<<grid, NTHREADS, smem, s>>>(B);
+  pw_tc_batch_pick(window_id, nt)<<<grid, NTHREADS, smem, s>>>(B);
   return cudaGetLastError();
 }
 // ---------------------------------------------------------------------------

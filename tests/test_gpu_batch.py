@@ -51,9 +51,10 @@ def test_batch_equals_standalone_plans(gpu):
     images = [torch.full_like(e, float("nan")) for e in expect]
     weights = [torch.full_like(w, float("nan")) if i % 2 == 0 else None for i, w in enumerate(expect_w)]
     batch = das.Batch(plans, rfs, images, weights=weights, n_streams=3)
-    # the compounded frames with 3+ angles (tensor-core kernel) share one persistent launch
+    # the compounded frames with 3+ angles (tensor-core kernel) go to persistent launches,
+    # one per pass width: 12-angle passes (11 and 3 angles) and 16-angle passes (31 angles)
     n_tc = sum(1 for p in plans if p.n_out == 1 and p.info()["kernel_variant"] == 9)
-    assert n_tc == 3 and batch.persistent() == (n_tc, 1)
+    assert n_tc == 3 and batch.persistent() == (n_tc, 2)
     for rep in range(2):                        # the graph is relaunched: same results
         for im in images:
             im.fill_(float("nan"))
@@ -132,10 +133,13 @@ def test_boundary_strategies_agree(gpu, win):
 @pytest.mark.parametrize("win", [windows.boxcar(), windows.hann(), windows.tukey(0.5), windows.triangular()],
                          ids=["boxcar", "hann", "tukey", "triangular"])
 def test_tensor_core_variant(gpu, win):
-    """Variant 9 (mma.sync with fp16 hi/lo operands) against variant 1 and the FP64 oracle."""
+    """Variant 9 (mma.sync with fp16 hi/lo operands) against variant 1 and the FP64 oracle.
+    Passes of 16 angles (4 mma n-tiles) where they take fewer passes than 12: 13, 31 and 49
+    angles (1, 2 and 4 passes); 36 angles runs three passes of 12."""
     import torch
     rng = np.random.default_rng(31)
-    for ne, na, nt, side in [(48, 11, 1024, 40), (45, 13, 768, 36), (36, 5, 512, 24), (29, 1, 512, 20)]:
+    for ne, na, nt, side in [(48, 11, 1024, 40), (45, 13, 768, 36), (36, 5, 512, 24), (29, 1, 512, 20),
+                             (24, 31, 512, 20), (20, 49, 384, 14), (16, 36, 384, 14)]:
         arr = synth.LinearArray(ne, PITCH, 0.918 * PITCH)
         px = (np.arange(side) - (side - 1) / 2.0) * PITCH / 3
         pz = 5e-3 + np.arange(side + 3) * PITCH / 3
