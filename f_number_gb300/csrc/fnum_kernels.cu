@@ -925,8 +925,9 @@ struct TcDerivShared {
 // dimage receives Draw (scaled like the image).
 //
 // BATCH (the persistent batch kernel, whose descriptor lies in global memory) reads the
-// descriptor fields of the bin loop once per tile; the per-frame kernels read their
-// parameters' fields where they are used (constant-bank operands, no registers held).
+// descriptor fields used at every bin (k_lb, tc_S) once per tile; the per-frame kernels
+// read their parameters' fields where they are used (constant-bank operands, no
+// registers held).
 template <int WIN, bool DERIV, bool BATCH = false, int NT = 3>
 __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles_x, int n_tiles_z, TcShared& sh,
                                            const dfl* lb_s, const dfl* ub_s, int* ktop, float2* __restrict__ image,
@@ -949,8 +950,7 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
   int4* seg_blk = d.seg + (size_t)blockIdx.x * NTHREADS * (size_t)d.seg_cap * PW_SEG_INT4;
   const float inv_par = (d.window_par > 0.0f) ? 1.0f / d.window_par : 0.0f;
   const float inv_sigma = 1.0f / tc_scale(*d.tc_max);
-  const int b_k_lb = d.k_lb, b_ne = d.ne, b_tc_S = d.tc_S;
-  const float b_window_par = d.window_par;
+  const int b_k_lb = d.k_lb, b_tc_S = d.tc_S;
 #define TC_D(field) (BATCH ? b_##field : d.field)
   const int tb = (d.tc_tb > 0 && d.tc_tb < TC_TB) ? d.tc_tb : TC_TB;   // bins per flush (a launch shape)
   constexpr int NA_P = 4 * NT;     // angles per pass
@@ -997,7 +997,7 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
       // or a half-width that is not positive) gets 1/L = 1e30, which sends its elements
       // to u >= 1 and keeps the other side's (distance 0 on this side) at u = d / L.
       float il = 1.0e30f, ir = 1.0e30f;
-      if (ilb < TC_D(ne)) {
+      if (ilb < d.ne) {
         const dfl l = lb_s[ilb];
         const float L = (bxm.x - l.x) + (bxm.y - l.y);
         if (L > 0.0f) il = __fdividef(1.0f, L);
@@ -1137,7 +1137,7 @@ __device__ __forceinline__ void pw_tc_tile(const PWDev& d, int tile, int n_tiles
                     for (int i = 0; i < 2; ++i) {
                       const float sd = s_dx[2 * TC_KS * V + 2 * s + i][tid];
                       const float u = fabsf(sd) * (sd < 0.0f ? en[V].y : en[V].z);
-                      bw[V][s][i] = (u < 1.0f) ? win_t<WIN>(TC_D(window_par), inv_par, u) * en[V].w : 0.0f;
+                      bw[V][s][i] = (u < 1.0f) ? win_t<WIN>(d.window_par, inv_par, u) * en[V].w : 0.0f;
                     }
                 }
               }
