@@ -312,7 +312,8 @@ int fnum_plan_set_shape(fnum_plan* plan, int blocks_per_sm, int bin_chunk);
    order of `plans`). */
 /* Compounded frames whose plans use the tensor-core kernel (variant 9) are not
    launched per frame: their band DFTs and spectra fragments run on the branches,
-   then ONE persistent launch per window type beamforms all of them -- each block
+   then ONE persistent launch per window type and pass width (12 or 16 angles
+   per pass) beamforms all of them -- each block
    draws tiles of all those frames from one counter, largest frames first, with
    each frame's descriptor read from device memory -- so no SM idles between
    frames.  The other frames keep a launch per frame on the other branches.
