@@ -1454,8 +1454,9 @@ static pw_kernel_t pw_pick_event_win(int window_id) {
 //     1: EPT 1 x NA 11   2: EPT 2 x NA 4   3: EPT 2 x NA 2   4: EPT 4 x NA 1
 //   boundaries resolved inside the bin loop (pw_fused_kernel):
 //     5: EPT 1 x NA 11   6: EPT 2 x NA 4   7: EPT 2 x NA 2   8: EPT 4 x NA 1
-//   9: tensor cores (pw_tc_kernel), 16 elements x 12 angles per pass; needs
-//      the plan's fragment scratch (PWDev::tc_B)
+//   9: tensor cores (pw_tc_kernel), 16 elements x 12 angles per pass, or 16
+//      angles where that takes fewer passes (PWDev::tc_nt); needs the plan's
+//      fragment scratch (PWDev::tc_B)
 // Angles beyond NA run as further passes inside the launch.  PWDev::variant
 // 0 picks by the angle count; a plan's autotuner may set another.
 static pw_kernel_t pw_pick_tc_win(int window_id, int nt) {

@@ -275,8 +275,9 @@ int fnum_das_pw_noalloc(const fnum_pw_desc* desc, const double* steering_angles,
    variant of a plane-wave plan on it (1: 1 element x 11 angles per pass,
    2: 2 x 4, 3: 2 x 2, 4: 4 x 1, with the segment boundaries resolved ahead of
    the bin loop; 5..8: the same shapes resolving them inside the bin loop;
-   9: tensor cores, 16 elements x 12 angles per pass, the default from 3
-   angles on) at full occupancy, and keeps the fastest
+   9: tensor cores, 16 elements x 12 angles per pass -- 16 angles where that
+   takes fewer passes -- the default from 3 angles on) at full occupancy, and
+   keeps the fastest
    for the plan's later executes.  It allocates a temporary image and runs on
    a private stream (not capturable).  variant / ms (the chosen variant's
    beamform time) may be NULL.  A synthetic-aperture plan times its two
