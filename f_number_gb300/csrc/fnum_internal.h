@@ -22,7 +22,7 @@ constexpr int KCHUNK = 64;
 constexpr int TC_TILE_X = 2;
 constexpr int TC_NA = 12;   // angles per angle pass (3 mma n-tiles of 4 complex angles)
 // A plane-wave plan's tensor-core kernel runs passes of 3 n-tiles (12 angles) or, when
-// that takes fewer passes (13-16, 25-32, 37-48 angles), of 4 (16 angles): each pass
+// that takes fewer passes (13-16, 25-32, 37-64 angles, ...), of 4 (16 angles): each pass
 // forms the same A operands, so fewer passes is less work.
 inline int tc_ntiles_for(int na) { return ((na + 15) / 16 < (na + TC_NA - 1) / TC_NA) ? 4 : 3; }
 constexpr int TC_EP = 16;   // elements per pass: TC_KS mma k-steps of 8 complex elements
