@@ -54,6 +54,12 @@ def test_membership_by_window_argument_matches_index_rule():
         want, c, ilb, iub, left = _index_rule(ne, M, pitch, width, x, h)
         got, u = _u_rule(ne, c, pitch, width, x, ilb, iub, left)
         assert np.array_equal(got, want), (ne, pitch, width, x, h)
+        # every member lies in [i_lb, i_ub]: the adjoint skips the warps whose elements
+        # miss that range for all of their voxels (a side without aperture, i_lb = ne or
+        # i_ub = -1, leaves the voxel beyond the array's end, with no element on the other
+        # side of it either)
+        e = np.arange(ne)
+        assert not np.any(want & ((e < ilb) | (e > iub))), (ne, pitch, width, x, h)
         finite = np.isfinite(u) & (u < 1e20)
         if finite.any():
             worst = min(worst, float(np.min(np.abs(u[finite] - 1.0))))
