@@ -662,6 +662,7 @@ def run_batch(args):
         torch.cuda.synchronize()
         solo.append(a.elapsed_time(b))
     batch = das.Batch(plans, rfs, imgs, n_streams=4)
+    n_persist_launches = batch.persistent()[1]
     for _ in range(args.warmup):
         batch.execute(stream)
     torch.cuda.synchronize()
@@ -692,10 +693,13 @@ def run_batch(args):
                           "in_batch_completion_p99": float(np.percentile(done, 99)),
                           "sum_of_standalone": float(np.sum(solo))},
            "clocks": clk,
-           # per frame: the band DFT (two kernels), then per beamform launch the kernel (+ scale
-           # and fragment kernels for the tensor-core variant)
-           "gpu_launches": args.steps * sum(2 + (1 if p.n_out == 1 else p.n_angles) * (3 if v == 9 else 1)
-                                            for p, v in zip(plans, variants))}
+           # per frame: the band DFT (two kernels); a compounded tensor-core frame then its
+           # scale and fragment kernels, its tiles beamformed by the persistent launches (one
+           # per window and pass width); any other frame per beamform launch the kernel (+
+           # scale and fragment kernels for the tensor-core variant)
+           "gpu_launches": args.steps * (n_persist_launches + sum(
+               2 + (2 if (p.n_out == 1 and v == 9) else (1 if p.n_out == 1 else p.n_angles) * (3 if v == 9 else 1))
+               for p, v in zip(plans, variants)))}
     print(json.dumps(out))
     batch.close()
     for p in plans:
